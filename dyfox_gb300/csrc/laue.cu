@@ -1,0 +1,499 @@
+// Laue march: per-angle constants, the general (interpolating) march, the
+// launch planner and the C entry points dyfox_laue_workspace_bytes /
+// dyfox_laue_solve (replacing laue/solver.py:34-118 and the three kernels of
+// laue/kernels.py).
+#include <math.h>
+#include <string.h>
+
+#include "laue_march.cuh"
+
+namespace dyfox {
+
+// cs staging, defined in volterra.cu.
+cudaError_t launch_cs_stage(bool single, const double *segs, int n_seg,
+                            int Nx, int Ny, int Nz, double dx,
+                            double dz, const VolterraConsts &vc, int row0,
+                            int n_rows, void *out, cudaStream_t stream);
+
+// ---------------------------------------------------------------------------
+// Per-(angle, step) constants of the interaction picture, in double:
+// kappa12_k, kappa21_k and the final factor M22^(Nz-1).  The step constants
+// cg, sg, e_p follow kernels.py:91-103.
+__device__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__global__ void laue_setup_kernel(const double *__restrict__ s_dev, int n_e,
+                                  int nsteps, double ds, double s0r,
+                                  double s0i, double shr, double shi,
+                                  double sbr, double sbi, Kappa *kappa,
+                                  double2 *scale) {
+    const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (idx >= (long)n_e * nsteps) return;
+    const int ie = (int)(idx / nsteps), k = (int)(idx - (long)ie * nsteps);
+    const double alpha = -2.0 * kPi * s_dev[ie];
+    const double gam = sqrt((shr * shr + shi * shi) + alpha * alpha * 0.25);
+    double cg, sg;
+    if (gam > 1e-30) {
+        cg = cos(gam * ds);
+        sg = sin(gam * ds) / gam;
+    } else {
+        cg = 1.0;
+        sg = ds;
+    }
+    const double p22i = alpha * 0.5 * sg;
+    const double rho = hypot(cg, p22i);
+    const double th = atan2(p22i, cg);
+    // e^{i (2k+1) th}: the product is split exactly (fma residual) so the
+    // phase carries no rounding growing with k.
+    const double m = 2.0 * k + 1.0;
+    const double ph = m * th;
+    const double pe = fma(m, th, -ph);
+    double sp, cp;
+    sincos(ph, &sp, &cp);
+    const double wr = cp - sp * pe, wi = sp + cp * pe;
+    const double f = sg / rho;
+    Kappa kp;
+    kp.k12 = make_double2(f * (sbr * wr - sbi * wi), f * (sbr * wi + sbi * wr));
+    kp.k21 = make_double2(f * (shr * wr + shi * wi), f * (shi * wr - shr * wi));
+    kappa[idx] = kp;
+    if (k == 0) {
+        const double exp_pr = exp(s0r * ds);
+        const double pi_ = (s0i + alpha * 0.5) * ds;
+        const double2 ep = make_double2(exp_pr * cos(pi_), exp_pr * sin(pi_));
+        double2 base = cmul(ep, make_double2(cg, p22i));
+        double2 acc = make_double2(1.0, 0.0);
+        for (int n = nsteps; n > 0; n >>= 1) {
+            if (n & 1) acc = cmul(acc, base);
+            base = cmul(base, base);
+        }
+        scale[ie] = acc;
+    }
+}
+
+// e^{iH(kk, x)} from a cheap source, for the general march.
+template <typename R>
+__device__ __forceinline__ typename RT<R>::R2 eval_cs(const MarchArgs &a,
+                                                      int iy, int row_blk,
+                                                      int kk, int x,
+                                                      const typename RT<R>::R2 *an_cs) {
+    const int Nx = a.Nx, Nz = a.Nz;
+    switch (a.hsrc) {
+    case HS_GRID64:
+        return CS<R>::of_f64(__ldg((const double *)a.hgrid +
+                                   ((size_t)iy * Nz + kk) * Nx + x));
+    case HS_GRID32:
+        return CS<R>::of_f32(__ldg((const float *)a.hgrid +
+                                   ((size_t)iy * Nz + kk) * Nx + x));
+    case HS_CS32:
+        return CS<R>::of_cs(__ldg((const float2 *)a.csgrid +
+                                  ((size_t)row_blk * (Nz - 1) + kk) * Nx + x));
+    case HS_CS64:
+        return CS<R>::of_cs(__ldg((const double2 *)a.csgrid +
+                                  ((size_t)row_blk * (Nz - 1) + kk) * Nx + x));
+    case HS_ANALYTIC:
+        return an_cs[kk];
+    default: {
+        typename RT<R>::R2 v;
+        v.x = R(1);
+        v.y = R(0);
+        return v;
+    }
+    }
+}
+
+// General march for any shift_px (laue/kernels.py:122-135 bilinear transport
+// with its edge rules), one CTA per (row, angle), state in shared memory,
+// in the same interaction picture as the register-resident march.
+template <typename R>
+__global__ void laue_general_kernel(const MarchArgs a, R shift_px) {
+    using R2 = typename RT<R>::R2;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int Nx = a.Nx, Nz = a.Nz, nsteps = Nz - 1, NP = Nx + 1;
+    R *st = reinterpret_cast<R *>(smem);
+    R2 *an_cs = reinterpret_cast<R2 *>(
+        smem + ((2 * 4 * (size_t)NP * sizeof(R) + 15) & ~(size_t)15));
+    const int row_blk = blockIdx.x / a.n_e, ie = blockIdx.x - row_blk * a.n_e;
+    const int iy = a.row0 + row_blk;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const double y_pix = (iy - a.Ny / 2) * a.dx;
+#define ST(b, c, i) st[((b) * 4 + (c)) * NP + (i)]
+    for (int ix = tid; ix < Nx; ix += nt) {
+        ST(0, 0, ix) = (R)beam_profile(ix, Nx, a.dx, a.sheet_hw);
+        ST(0, 1, ix) = 0; ST(0, 2, ix) = 0; ST(0, 3, ix) = 0;
+    }
+    if (a.hsrc == HS_ANALYTIC)
+        for (int k = tid; k < nsteps; k += nt)
+            an_cs[k] = CS<R>::of_f64(analytic_h(a.an, y_pix, k, a.dz));
+    __syncthreads();
+    int cur = 0;
+    const Kappa *kap = a.kappa + (size_t)ie * nsteps;
+    for (int k = 0; k < nsteps; ++k) {
+        const int nx = 1 - cur;
+        const Kappa kk4 = ldg_kappa(kap + k);
+        const R k12r = (R)kk4.k12.x, k12i = (R)kk4.k12.y;
+        const R k21r = (R)kk4.k21.x, k21i = (R)kk4.k21.y;
+        for (int ix = tid; ix < Nx; ix += nt) {
+            const R2 e = eval_cs<R>(a, iy, row_blk, k, ix, an_cs);
+            R src0 = (R)ix + shift_px;
+            int i0 = (int)floor(src0);
+            R f0 = src0 - (R)i0, ar, ai;
+            if (i0 >= 0 && i0 + 1 < Nx) {
+                ar = (1 - f0) * ST(cur, 0, i0) + f0 * ST(cur, 0, i0 + 1);
+                ai = (1 - f0) * ST(cur, 1, i0) + f0 * ST(cur, 1, i0 + 1);
+            } else if (i0 >= 0 && i0 < Nx) {
+                ar = (1 - f0) * ST(cur, 0, i0);
+                ai = (1 - f0) * ST(cur, 1, i0);
+            } else {
+                ar = 0; ai = 0;
+            }
+            R srcg = (R)ix - shift_px;
+            int ig = (int)floor(srcg);
+            R fg = srcg - (R)ig, br, bi;
+            if (ig >= 0 && ig + 1 < Nx) {
+                br = (1 - fg) * ST(cur, 2, ig) + fg * ST(cur, 2, ig + 1);
+                bi = (1 - fg) * ST(cur, 3, ig) + fg * ST(cur, 3, ig + 1);
+            } else if (ig >= 0 && ig < Nx) {
+                br = (1 - fg) * ST(cur, 2, ig);
+                bi = (1 - fg) * ST(cur, 3, ig);
+            } else {
+                br = 0; bi = 0;
+            }
+            const R m12r = k12r * e.x - k12i * e.y, m12i = k12r * e.y + k12i * e.x;
+            const R m21r = k21r * e.x + k21i * e.y, m21i = k21i * e.x - k21r * e.y;
+            ST(nx, 0, ix) = fmaR(m12r, br, fmaR(-m12i, bi, ar));
+            ST(nx, 1, ix) = fmaR(m12r, bi, fmaR(m12i, br, ai));
+            ST(nx, 2, ix) = fmaR(m21r, ar, fmaR(-m21i, ai, br));
+            ST(nx, 3, ix) = fmaR(m21r, ai, fmaR(m21i, ar, bi));
+        }
+        __syncthreads();
+        cur = nx;
+    }
+    const double2 S = __ldg(a.scale + ie);
+    R2 *out = reinterpret_cast<R2 *>(a.out) + ((size_t)ie * a.Ny + iy) * Nx;
+    for (int ix = tid; ix < Nx; ix += nt) {
+        const double br = ST(cur, 2, ix), bi = ST(cur, 3, ix);
+        out[ix] = R2{(R)(S.x * br - S.y * bi), (R)(S.x * bi + S.y * br)};
+    }
+#undef ST
+}
+
+// Rows with |y| >= fov_hy are written as zero (kernels.py:70-75).
+__global__ void zero_rows_kernel(char *out, int n_e, int Ny, size_t row_bytes,
+                                 int row0, int n_rows) {
+    const int n_inactive = Ny - n_rows;
+    const long r = blockIdx.y;                 // (angle, inactive row)
+    const int ie = (int)(r / n_inactive), j = (int)(r - (long)ie * n_inactive);
+    const int iy = j < row0 ? j : j + n_rows;
+    uint4 *p = reinterpret_cast<uint4 *>(out + ((size_t)ie * Ny + iy) * row_bytes);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+         i < row_bytes / 16; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = make_uint4(0, 0, 0, 0);
+}
+
+// ---------------------------------------------------------------------------
+struct LauePlan {
+    bool general = false;
+    int hsrc = HS_NONE;      // source the march kernel reads
+    int stage = 0;           // 0: none, 1: stage e^{iH} (CS32/CS64)
+    int row0 = 0, n_rows = 0;
+    size_t off_kappa = 0, off_scale = 0, off_stage = 0, ws = 0;
+};
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static int validate(const dyfox_laue_desc *d) {
+    if (!d) { set_error("descriptor is NULL"); return DYFOX_EINVAL; }
+    if (d->Nx < 1 || d->Ny < 1 || d->Nz < 2 || d->n_e < 1) {
+        set_error("bad sizes Nx=%d Ny=%d Nz=%d n_e=%d (need Nx, Ny, n_e >= 1, "
+                  "Nz >= 2)", d->Nx, d->Ny, d->Nz, d->n_e);
+        return DYFOX_EINVAL;
+    }
+    if (d->precision != DYFOX_FP64 && d->precision != DYFOX_FP32) {
+        set_error("precision is DYFOX_FP64 or DYFOX_FP32, not %d", d->precision);
+        return DYFOX_EINVAL;
+    }
+    if (!(d->dx > 0) || !(d->dz > 0) || !(d->ds > 0) || !(d->shift_px > 0) ||
+        !isfinite(d->shift_px) || !isfinite(d->sheet_hw) || d->sheet_hw == 0.0) {
+        set_error("bad grid scalars dx=%g dz=%g ds=%g shift_px=%g sheet_hw=%g",
+                  d->dx, d->dz, d->ds, d->shift_px, d->sheet_hw);
+        return DYFOX_EINVAL;
+    }
+    if (d->h_source < DYFOX_H_NONE || d->h_source > DYFOX_H_ANALYTIC) {
+        set_error("unknown h_source %d", d->h_source);
+        return DYFOX_EINVAL;
+    }
+    if (d->h_source == DYFOX_H_SEGMENTS && d->n_seg < 0) {
+        set_error("n_seg < 0");
+        return DYFOX_EINVAL;
+    }
+    const double *sc[] = {d->sig0, d->sig_h, d->sig_hbar};
+    for (int i = 0; i < 3; ++i)
+        if (!isfinite(sc[i][0]) || !isfinite(sc[i][1])) {
+            set_error("non-finite crystal coupling");
+            return DYFOX_ENAN;
+        }
+    return DYFOX_OK;
+}
+
+static void active_rows(const dyfox_laue_desc *d, int *row0, int *n_rows) {
+    int first = -1, count = 0;
+    for (int iy = 0; iy < d->Ny; ++iy) {
+        double y_pix = (iy - d->Ny / 2) * d->dx;
+        if (fabs(y_pix) < d->fov_hy) {
+            if (first < 0) first = iy;
+            ++count;
+        }
+    }
+    *row0 = first < 0 ? 0 : first;
+    *n_rows = count;
+}
+
+static int make_plan(const dyfox_laue_desc *d, LauePlan *p) {
+    int st = validate(d);
+    if (st) return st;
+    active_rows(d, &p->row0, &p->n_rows);
+    const bool exact = d->shift_px == 1.0;
+    p->general = !exact || (d->flags & DYFOX_FLAG_GENERAL);
+    const bool single = d->precision == DYFOX_FP32;
+    switch (d->h_source) {
+    case DYFOX_H_NONE: p->hsrc = HS_NONE; break;
+    case DYFOX_H_GRID_F64: p->hsrc = HS_GRID64; break;
+    case DYFOX_H_GRID_F32: p->hsrc = HS_GRID32; break;
+    case DYFOX_H_ANALYTIC: p->hsrc = HS_ANALYTIC; break;
+    default: {
+        bool fused;
+        if (d->flags & DYFOX_FLAG_FUSED) fused = true;
+        else if (d->flags & DYFOX_FLAG_STAGED) fused = false;
+        else fused = d->n_e <= 8;   // one CTA can hold every angle
+        if (p->general) fused = false;
+        if (d->n_seg == 0) { p->hsrc = HS_NONE; break; }
+        p->hsrc = fused ? HS_SEG : (single ? HS_CS32 : HS_CS64);
+        p->stage = fused ? 0 : 1;
+    }
+    }
+    size_t off = 0;
+    p->off_kappa = off;
+    off = align256(off + (size_t)d->n_e * (d->Nz - 1) * sizeof(Kappa));
+    p->off_scale = off;
+    off = align256(off + (size_t)d->n_e * sizeof(double2));
+    p->off_stage = off;
+    if (p->stage)
+        off = align256(off + (size_t)p->n_rows * (d->Nz - 1) * d->Nx *
+                                 (single ? sizeof(float2) : sizeof(double2)));
+    p->ws = off;
+    return DYFOX_OK;
+}
+
+struct FastConfig {
+    MarchEntry entry;
+    int cpl, WA, A, block;
+    size_t smem;
+};
+
+static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
+                       FastConfig *fc) {
+    const bool single = d->precision == DYFOX_FP32;
+    const bool comp = single && !(d->flags & DYFOX_FLAG_NO_COMP);
+    const int ht = p.hsrc == HS_SEG ? HT_SEG : HT_GENERIC;
+    const int *cpls = single ? kCplF32 : kCplF64;
+    const int ncpl = single ? kNumCplF32 : kNumCplF64;
+    // Columns per lane: the fewest padded columns; ties go to more columns
+    // per lane (fewer warps per angle).
+    int best = -1, best_pad = 1 << 30;
+    for (int i = 0; i < ncpl; ++i) {
+        int c = cpls[i];
+        if (d->cols_per_lane && c != d->cols_per_lane) continue;
+        int wa = div_up(d->Nx, 32 * c);
+        int pad = wa * 32 * c - d->Nx;
+        if (wa > 32) continue;
+        if (pad < best_pad || (pad == best_pad && c > best)) {
+            best = c;
+            best_pad = pad;
+        }
+    }
+    if (best < 0) {
+        set_error("no register-resident configuration for Nx=%d "
+                  "(cols_per_lane=%d)", d->Nx, d->cols_per_lane);
+        return DYFOX_ENOSYS;
+    }
+    fc->cpl = best;
+    fc->WA = div_up(d->Nx, 32 * best);
+    fc->entry = single ? (comp ? march_entry_f32_comp(best, ht)
+                               : march_entry_f32_plain(best, ht))
+                       : march_entry_f64(best, ht);
+    if (!fc->entry.launch) {
+        set_error("missing instantiation cpl=%d", best);
+        return DYFOX_ENOSYS;
+    }
+    cudaFuncAttributes attr;
+    cudaError_t e = fc->entry.attr(&attr);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncGetAttributes(march)");
+    int max_threads = attr.maxThreadsPerBlock < 1024 ? attr.maxThreadsPerBlock
+                                                     : 1024;
+    int cap = 512 < max_threads ? 512 : max_threads;
+    int amax = cap / (32 * fc->WA);
+    if (amax < 1) amax = max_threads / (32 * fc->WA);
+    if (amax < 1) {
+        set_error("Nx=%d needs %d warps per angle, above the block limit",
+                  d->Nx, fc->WA);
+        return DYFOX_ENOSYS;
+    }
+    int A = d->angles_per_cta > 0 ? d->angles_per_cta : d->n_e;
+    if (A > amax) A = amax;
+    if (A > d->n_e) A = d->n_e;
+    if (A * 32 * fc->WA > max_threads) {
+        set_error("angles_per_cta=%d exceeds the block limit", A);
+        return DYFOX_EINVAL;
+    }
+    fc->A = A;
+    fc->block = 32 * fc->WA * A;
+    MarchSmem sm = single
+        ? march_smem<float>(best, fc->WA, A, d->Nz, p.hsrc, d->n_seg, comp)
+        : march_smem<double>(best, fc->WA, A, d->Nz, p.hsrc, d->n_seg, false);
+    fc->smem = sm.total;
+    return DYFOX_OK;
+}
+
+static int smem_limit(size_t need) {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&optin,
+                                   cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return cuda_status(e, "device query");
+    if (need > (size_t)optin) {
+        set_error("kernel needs %zu bytes of shared memory per block, the device "
+                  "allows %d", need, optin);
+        return DYFOX_ESMEM;
+    }
+    return DYFOX_OK;
+}
+
+}  // namespace dyfox
+
+using namespace dyfox;
+
+extern "C" size_t dyfox_laue_workspace_bytes(const dyfox_laue_desc *d) {
+    LauePlan p;
+    if (make_plan(d, &p)) return 0;
+    return p.ws;
+}
+
+extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
+                                const void *h_grid, const double *seg_table,
+                                void *out, void *workspace,
+                                size_t workspace_bytes, void *stream_) {
+    set_error("");
+    LauePlan p;
+    int st = make_plan(d, &p);
+    if (st) return st;
+    if (!s_dev || !out) {
+        set_error("s_dev and out must be device pointers");
+        return DYFOX_EINVAL;
+    }
+    if ((d->h_source == DYFOX_H_GRID_F64 || d->h_source == DYFOX_H_GRID_F32) &&
+        !h_grid) {
+        set_error("h_source is a grid but h_grid is NULL");
+        return DYFOX_EINVAL;
+    }
+    if (d->h_source == DYFOX_H_SEGMENTS && d->n_seg > 0 && !seg_table) {
+        set_error("h_source is segments but seg_table is NULL");
+        return DYFOX_EINVAL;
+    }
+    if (workspace_bytes < p.ws || (p.ws && !workspace)) {
+        set_error("workspace of %zu bytes, %zu needed", workspace_bytes, p.ws);
+        return DYFOX_ENOMEM;
+    }
+    cudaStream_t stream = (cudaStream_t)stream_;
+    const bool single = d->precision == DYFOX_FP32;
+    const size_t elem = single ? sizeof(float2) : sizeof(double2);
+    char *ws = (char *)workspace;
+    const int nsteps = d->Nz - 1;
+
+    MarchArgs a;
+    memset(&a, 0, sizeof a);
+    a.Nx = d->Nx; a.Ny = d->Ny; a.Nz = d->Nz; a.n_e = d->n_e;
+    a.row0 = p.row0; a.n_rows = p.n_rows;
+    a.dx = d->dx; a.dz = d->dz; a.sheet_hw = d->sheet_hw;
+    a.hsrc = p.hsrc;
+    a.hgrid = h_grid;
+    a.segs = seg_table;
+    a.n_seg = d->h_source == DYFOX_H_SEGMENTS ? d->n_seg : 0;
+    a.vc = volterra_consts(d->nu, d->a_core);
+    memcpy(a.an, d->analytic, sizeof a.an);
+    a.kappa = (const Kappa *)(ws + p.off_kappa);
+    a.scale = (const double2 *)(ws + p.off_scale);
+    a.out = out;
+    a.csgrid = ws + p.off_stage;
+
+    cudaError_t e;
+    // Rows outside the beam are zero.
+    if (p.n_rows < d->Ny) {
+        size_t row_bytes = (size_t)d->Nx * elem;
+        dim3 grid(div_up((int)(row_bytes / 16), 256) < 64
+                      ? div_up((int)(row_bytes / 16), 256) : 64,
+                  d->n_e * (d->Ny - p.n_rows));
+        zero_rows_kernel<<<grid, 256, 0, stream>>>((char *)out, d->n_e, d->Ny,
+                                                   row_bytes, p.row0, p.n_rows);
+        count_launch(1);
+        if ((e = cudaGetLastError())) return cuda_status(e, "zero_rows");
+    }
+    if (p.n_rows == 0) return DYFOX_OK;
+
+    {
+        long n = (long)d->n_e * nsteps;
+        laue_setup_kernel<<<(int)((n + 255) / 256), 256, 0, stream>>>(
+            s_dev, d->n_e, nsteps, d->ds, d->sig0[0], d->sig0[1], d->sig_h[0],
+            d->sig_h[1], d->sig_hbar[0], d->sig_hbar[1],
+            (Kappa *)(ws + p.off_kappa), (double2 *)(ws + p.off_scale));
+        count_launch(1);
+        if ((e = cudaGetLastError())) return cuda_status(e, "laue_setup");
+    }
+    if (p.stage) {
+        e = launch_cs_stage(single, seg_table, d->n_seg, d->Nx, d->Ny,
+                            d->Nz, d->dx, d->dz, a.vc, p.row0, p.n_rows,
+                            ws + p.off_stage, stream);
+        if (e) return cuda_status(e, "cs_stage");
+    }
+
+    if (p.general) {
+        size_t smem = ((2 * 4 * (size_t)(d->Nx + 1) * (single ? 4 : 8) + 15) &
+                       ~(size_t)15) +
+                      (p.hsrc == HS_ANALYTIC ? (size_t)d->Nz * elem : 0);
+        if ((st = smem_limit(smem))) return st;
+        a.n_groups = d->n_e;
+        a.A = 1;
+        int grid = p.n_rows * d->n_e;
+        if (single) {
+            auto *k = laue_general_kernel<float>;
+            if (smem > 48 * 1024 &&
+                (e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem)))
+                return cuda_status(e, "general smem");
+            k<<<grid, 256, smem, stream>>>(a, (float)d->shift_px);
+            count_launch(1);
+        } else {
+            auto *k = laue_general_kernel<double>;
+            if (smem > 48 * 1024 &&
+                (e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem)))
+                return cuda_status(e, "general smem");
+            k<<<grid, 256, smem, stream>>>(a, d->shift_px);
+            count_launch(1);
+        }
+        if ((e = cudaGetLastError())) return cuda_status(e, "laue_general");
+        return DYFOX_OK;
+    }
+
+    FastConfig fc;
+    if ((st = choose_fast(d, p, &fc))) return st;
+    if ((st = smem_limit(fc.smem))) return st;
+    a.WA = fc.WA;
+    a.A = fc.A;
+    a.ncols = 32 * fc.WA * fc.cpl;
+    a.n_groups = div_up(d->n_e, fc.A);
+    e = fc.entry.launch(a, p.n_rows * a.n_groups, fc.block, fc.smem, stream);
+    if (e) return cuda_status(e, "laue_march");
+    return DYFOX_OK;
+}

@@ -1,0 +1,469 @@
+// Takagi-Taupin depth march of the Laue geometry (DYFOX laue/kernels.py
+// 48-352), register-resident, for exact advection (shift_px == 1).
+//
+// The reference update per depth step k (kernels.py:95-141) is
+//   D0'(x) = M11 D0(x+1) + M12(x) Dg(x-1)
+//   Dg'(x) = M21(x) D0(x+1) + M22 Dg(x-1)
+// with M = e_p P, P11 = cg - i(a/2)sg, P22 = cg + i(a/2)sg = rho e^{i th},
+// M12 = e_p sg sigma_hbar e^{+iH(k,x)}, M21 = e_p sg sigma_h e^{-iH(k,x)},
+// zero fill beyond both edges.  The march here runs in the interaction
+// picture D0_k = (e_p rho)^k e^{-ik th} A_k, Dg_k = (e_p rho)^k e^{ik th} B_k:
+//   A'(x) = A(x+1) + kappa12_k e^{+iH} B(x-1)
+//   B'(x) = B(x-1) + kappa21_k e^{-iH} A(x+1)
+// kappa12_k = (sg/rho) sigma_hbar e^{i(2k+1)th},
+// kappa21_k = (sg/rho) sigma_h e^{-i(2k+1)th},
+// and D_g(t) = M22^(Nz-1) B_(Nz-1).  Mathematically identical; the diagonal
+// becomes an exact shift (no rounding drift in single precision) and a step
+// costs 16 real FMA-class operations per column instead of 24.
+//
+// Work layout: one CTA per (grid row, group of `A` deviation parameters).
+// Each angle owns WA warps; lane L of an angle holds the CPL contiguous
+// columns [L*CPL, (L+1)*CPL) of A and B in registers.  The one-column shift
+// moves in registers, across lanes by warp shuffle and across warps through
+// a double-buffered shared-memory boundary slot; one __syncthreads per step.
+// e^{iH(k,.)} for the row is produced once per CTA per step into a
+// double-buffered shared-memory row (all angles of the CTA share it) while
+// the previous step is consumed.
+#pragma once
+#include "common.cuh"
+#include "volterra.cuh"
+
+namespace dyfox {
+
+enum HSrc { HS_NONE = 0, HS_GRID64 = 1, HS_GRID32 = 2, HS_CS32 = 3,
+            HS_SEG = 4, HS_ANALYTIC = 5, HS_CS64 = 6 };
+enum HTemplate { HT_GENERIC = 0, HT_SEG = 1 };
+
+// Interaction-picture coupling constants of one (angle, step).
+struct Kappa {
+    double2 k12, k21;
+};
+
+__device__ __forceinline__ Kappa ldg_kappa(const Kappa *p) {
+    Kappa k;
+    k.k12 = __ldg(&p->k12);
+    k.k21 = __ldg(&p->k21);
+    return k;
+}
+
+struct MarchArgs {
+    int Nx, Ny, Nz, n_e;
+    int WA, A, ncols, n_groups;
+    int row0, n_rows;
+    double dx, dz, sheet_hw;
+    int hsrc;
+    const void *hgrid;          // GRID64 / GRID32: (Ny, Nz, Nx)
+    const void *csgrid;         // CS32 / CS64: staged e^{iH} as float2 /
+                                // double2, (n_rows, Nz - 1, Nx), row-relative
+    const double *segs;         // SEG: segment table
+    int n_seg;
+    VolterraConsts vc;
+    double an[12];              // ANALYTIC
+    const Kappa *kappa;         // (n_e, Nz - 1): kappa12, kappa21
+    const double2 *scale;       // (n_e): M22^(Nz-1)
+    void *out;                  // (n_e, Ny, Nx) complex (R2)
+};
+
+// Input beam D0(z=0) at column x (kernels.py:77-88), in double.
+__device__ __forceinline__ double beam_profile(int x, int Nx, double dx,
+                                               double sheet_hw) {
+    double x_pos = (x - Nx / 2) * dx;
+    return sheet_hw > 0.0 ? (fabs(x_pos) < sheet_hw ? 1.0 : 0.0)
+                          : exp(-x_pos * x_pos / (2.0 * sheet_hw * sheet_hw));
+}
+
+// Closed-form H(y, z_k) of a single line along x (kernels.py:216-228).
+__device__ __forceinline__ double analytic_h(const double *an, double y_pix,
+                                             int k, double dz) {
+    double dy = y_pix - an[0];
+    double onu = 1.0 - an[10];
+    double c1 = an[9] / (2.0 * kPi);
+    double dzv = k * dz - an[1];
+    double d1 = dy * an[2] + dzv * an[3];
+    double d2 = dy * an[4] + dzv * an[5];
+    double r2 = d1 * d1 + d2 * d2;
+    double r2c = (r2 > an[11]) ? r2 : an[11];
+    double H = an[6] * atan2(d2, d1);
+    if (an[9] > 0.0) {
+        double nu = an[10];
+        double ux = c1 * d1 * d2 / (2.0 * onu * r2c);
+        double uy = -c1 * ((1.0 - 2.0 * nu) / (4.0 * onu) * log(r2c)
+                           + (d1 * d1 - d2 * d2) / (4.0 * onu * r2c));
+        H += 2.0 * kPi * (an[7] * ux + an[8] * uy);
+    }
+    return H;
+}
+
+template <typename R> struct CS;
+template <> struct CS<double> {
+    static __device__ __forceinline__ double2 of_f64(double h) {
+        double s, c;
+        sincos(h, &s, &c);
+        return make_double2(c, s);
+    }
+    static __device__ __forceinline__ double2 of_f32(float h) {
+        return of_f64((double)h);
+    }
+    static __device__ __forceinline__ double2 of_cs(float2 v) {
+        return make_double2(v.x, v.y);
+    }
+    static __device__ __forceinline__ double2 of_cs(double2 v) { return v; }
+};
+template <> struct CS<float> {
+    static __device__ __forceinline__ float2 of_f64(double h) {
+        float s, c;
+        sincosf(reduce_2pi(h), &s, &c);
+        return make_float2(c, s);
+    }
+    static __device__ __forceinline__ float2 of_f32(float h) {
+        float s, c;
+        sincosf(h, &s, &c);
+        return make_float2(c, s);
+    }
+    static __device__ __forceinline__ float2 of_cs(float2 v) { return v; }
+    static __device__ __forceinline__ float2 of_cs(double2 v) {
+        return make_float2((float)v.x, (float)v.y);
+    }
+};
+
+// Knuth's error-free sum: s + err == a + b exactly (round to nearest).
+template <typename R>
+__device__ __forceinline__ R two_sum(R a, R b, R &err) {
+    R s = a + b;
+    R bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+    return s;
+}
+
+__device__ __forceinline__ double fmaR(double a, double b, double c) {
+    return fma(a, b, c);
+}
+__device__ __forceinline__ float fmaR(float a, float b, float c) {
+    return fmaf(a, b, c);
+}
+
+// Shared-memory plan of the march kernel (bytes), shared with the host.
+struct MarchSmem {
+    size_t cs, bnd, an, segf, piv, hc, total;
+};
+
+template <typename R>
+__host__ __device__ inline MarchSmem march_smem(int CPL, int WA, int A,
+                                                int Nz, int hsrc, int n_seg,
+                                                bool comp) {
+    using R2 = typename RT<R>::R2;
+    MarchSmem m;
+    int PS = 32 * WA + 1;
+    int nwarps = WA * A;
+    m.cs = 0;
+    size_t off = (size_t)2 * CPL * PS * sizeof(R2);
+    m.bnd = off;
+    off += (size_t)2 * nwarps * (comp ? 4 : 2) * sizeof(R2);
+    off = (off + 15) & ~(size_t)15;
+    m.an = off;
+    if (hsrc == HS_ANALYTIC) off += (size_t)Nz * sizeof(R2);
+    off = (off + 15) & ~(size_t)15;
+    m.segf = off;
+    if (hsrc == HS_SEG && sizeof(R) == 4) off += (size_t)n_seg * sizeof(SegF);
+    off = (off + 15) & ~(size_t)15;
+    m.piv = off;
+    if (hsrc == HS_SEG && sizeof(R) == 4)
+        off += (size_t)2 * n_seg * sizeof(float4);
+    m.hc = off;
+    off += sizeof(double);
+    m.total = off;
+    return m;
+}
+
+template <typename R, int CPL, int HT, bool COMP>
+__global__ void laue_march_kernel(const MarchArgs a) {
+    using R2 = typename RT<R>::R2;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int WA = a.WA;
+    const int PS = 32 * WA + 1;
+    const int nthreads = blockDim.x;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nwarps = nthreads >> 5;
+    const int g = warp / WA, wa = warp - g * WA;
+    const int L = wa * 32 + lane;
+    const int row_blk = blockIdx.x / a.n_groups;
+    const int grp = blockIdx.x - row_blk * a.n_groups;
+    const int iy = a.row0 + row_blk;
+    const int ie_raw = grp * a.A + g;
+    const int ie = ie_raw < a.n_e ? ie_raw : a.n_e - 1;
+    const int Nx = a.Nx, Nz = a.Nz, nsteps = Nz - 1;
+    const int hsrc = HT == HT_SEG ? HS_SEG : a.hsrc;
+    const MarchSmem plan = march_smem<R>(CPL, WA, a.A, Nz, hsrc, a.n_seg,
+                                         COMP);
+    R2 *cs = reinterpret_cast<R2 *>(smem + plan.cs);
+    R2 *bnd = reinterpret_cast<R2 *>(smem + plan.bnd);
+    R2 *an_cs = reinterpret_cast<R2 *>(smem + plan.an);
+    SegF *segf = reinterpret_cast<SegF *>(smem + plan.segf);
+    float4 *piv = reinterpret_cast<float4 *>(smem + plan.piv);
+    double *hc_sm = reinterpret_cast<double *>(smem + plan.hc);
+    const int NB = COMP ? 4 : 2;
+    const double y_pix = (iy - a.Ny / 2) * a.dx;
+    constexpr bool kSingle = sizeof(R) == 4;
+
+    // ---------------------------------------------------------- prologue
+    if (HT == HT_SEG && kSingle) {
+        if (tid == 0) *hc_sm = sum_hconst(a.segs, a.n_seg);
+        for (int s = tid; s < a.n_seg; s += nthreads) {
+            const double *sg = a.segs + (size_t)s * DYFOX_SEG_STRIDE;
+            segf[s] = seg_f32(sg);
+            piv[s] = seg_pivot(sg, y_pix, 0.0, Nx, a.dx);
+            if (nsteps > 1)
+                piv[a.n_seg + s] = seg_pivot(sg, y_pix, a.dz, Nx, a.dx);
+        }
+    }
+    if (HT == HT_GENERIC && hsrc == HS_ANALYTIC) {
+        for (int k = tid; k < nsteps; k += nthreads)
+            an_cs[k] = CS<R>::of_f64(analytic_h(a.an, y_pix, k, a.dz));
+    }
+    if ((HT == HT_SEG && kSingle) || hsrc == HS_ANALYTIC) __syncthreads();
+    // Sum over segments of the constant the single evaluator drops.
+    double hconst = 0.0;
+    if (HT == HT_SEG && kSingle) hconst = *hc_sm;
+
+    // Produces e^{iH(kk, x)} of every padded column into buffer `buf`.
+    auto produce = [&](int kk, int buf) {
+        R2 *dst = cs + (size_t)buf * CPL * PS;
+#pragma unroll
+        for (int i = 0; i < CPL; ++i) {
+            const int x = tid + i * nthreads;
+            if (x >= a.ncols) continue;
+            R2 v;
+            if (x >= Nx) {
+                v.x = R(0); v.y = R(0);
+            } else if (HT == HT_SEG) {
+                if (kSingle) {
+                    const float4 *pv = piv + (size_t)(kk & 1) * a.n_seg;
+                    double acc = hconst;
+                    for (int s = 0; s < a.n_seg; ++s)
+                        acc += (double)h_seg_f32(segf[s], pv[s], x);
+                    v = CS<R>::of_f64(acc);
+                } else {
+                    const double X0 = __dmul_rn((double)x - 0.5 * Nx, a.dx);
+                    const double yv = __dmul_rn((double)iy - 0.5 * a.Ny, a.dx);
+                    const double zv = __dmul_rn((double)kk, a.dz);
+                    double acc = 0.0;
+                    for (int s = 0; s < a.n_seg; ++s) {
+                        const double *sg = a.segs + (size_t)s * DYFOX_SEG_STRIDE;
+                        acc = __dadd_rn(acc, h_seg_f64(
+                            sg, __dsub_rn(X0, __ldg(sg + SEG_CX)),
+                            __dsub_rn(yv, __ldg(sg + SEG_CY)),
+                            __dsub_rn(zv, __ldg(sg + SEG_CZ)), a.vc));
+                    }
+                    v = CS<R>::of_f64(acc);
+                }
+            } else {
+                switch (hsrc) {
+                case HS_GRID64:
+                    v = CS<R>::of_f64(__ldg(
+                        (const double *)a.hgrid +
+                        ((size_t)iy * Nz + kk) * Nx + x));
+                    break;
+                case HS_GRID32:
+                    v = CS<R>::of_f32(__ldg(
+                        (const float *)a.hgrid +
+                        ((size_t)iy * Nz + kk) * Nx + x));
+                    break;
+                case HS_CS32:
+                    v = CS<R>::of_cs(__ldg(
+                        (const float2 *)a.csgrid +
+                        ((size_t)row_blk * nsteps + kk) * Nx + x));
+                    break;
+                case HS_CS64:
+                    v = CS<R>::of_cs(__ldg(
+                        (const double2 *)a.csgrid +
+                        ((size_t)row_blk * nsteps + kk) * Nx + x));
+                    break;
+                case HS_ANALYTIC:
+                    v = an_cs[kk];
+                    break;
+                default:
+                    v.x = R(1); v.y = R(0);
+                }
+            }
+            dst[(x % CPL) * PS + x / CPL] = v;
+        }
+    };
+
+    // Initial state: A = input beam, B = 0.
+    R Ar[CPL], Ai[CPL], Br[CPL], Bi[CPL];
+    R Alr[COMP ? CPL : 1], Ali[COMP ? CPL : 1], Blr[COMP ? CPL : 1],
+        Bli[COMP ? CPL : 1];
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) {
+        const int x = L * CPL + j;
+        Ar[j] = x < Nx ? (R)beam_profile(x, Nx, a.dx, a.sheet_hw) : R(0);
+        Ai[j] = R(0); Br[j] = R(0); Bi[j] = R(0);
+        if constexpr (COMP) { Alr[j] = 0; Ali[j] = 0; Blr[j] = 0; Bli[j] = 0; }
+    }
+    produce(0, 0);
+    if (lane == 0) {
+        bnd[(0 * nwarps + warp) * NB + 0] = R2{Ar[0], Ai[0]};
+        if constexpr (COMP) bnd[(0 * nwarps + warp) * NB + 2] = R2{Alr[0], Ali[0]};
+    }
+    if (lane == 31) {
+        bnd[(0 * nwarps + warp) * NB + 1] = R2{Br[CPL - 1], Bi[CPL - 1]};
+        if constexpr (COMP) bnd[(0 * nwarps + warp) * NB + 3] = R2{Blr[CPL - 1], Bli[CPL - 1]};
+    }
+    __syncthreads();
+
+    const Kappa *kap = a.kappa + (size_t)ie * nsteps;
+    Kappa kn = ldg_kappa(kap);
+    // ------------------------------------------------------------ march
+    for (int k = 0; k < nsteps; ++k) {
+        const int p = k & 1;
+        const Kappa kk4 = kn;
+        if (k + 1 < nsteps) kn = ldg_kappa(kap + k + 1);
+        if (HT == HT_SEG && kSingle && k + 2 < nsteps) {
+            for (int s = tid; s < a.n_seg; s += nthreads)
+                piv[(size_t)(k & 1) * a.n_seg + s] = seg_pivot(
+                    a.segs + (size_t)s * DYFOX_SEG_STRIDE, y_pix,
+                    (k + 2) * a.dz, Nx, a.dx);
+        }
+        if (k + 1 < nsteps) produce(k + 1, p ^ 1);
+
+        const R k12r = (R)kk4.k12.x, k12i = (R)kk4.k12.y;
+        const R k21r = (R)kk4.k21.x, k21i = (R)kk4.k21.y;
+        // Neighbour values of the previous state.
+        R ainr = __shfl_down_sync(0xffffffffu, Ar[0], 1);
+        R aini = __shfl_down_sync(0xffffffffu, Ai[0], 1);
+        R binr = __shfl_up_sync(0xffffffffu, Br[CPL - 1], 1);
+        R bini = __shfl_up_sync(0xffffffffu, Bi[CPL - 1], 1);
+        R ainlr = 0, ainli = 0, binlr = 0, binli = 0;
+        if constexpr (COMP) {
+            ainlr = __shfl_down_sync(0xffffffffu, Alr[0], 1);
+            ainli = __shfl_down_sync(0xffffffffu, Ali[0], 1);
+            binlr = __shfl_up_sync(0xffffffffu, Blr[CPL - 1], 1);
+            binli = __shfl_up_sync(0xffffffffu, Bli[CPL - 1], 1);
+        }
+        if (lane == 31) {
+            if (wa + 1 < WA) {
+                R2 t = bnd[(p * nwarps + warp + 1) * NB + 0];
+                ainr = t.x; aini = t.y;
+                if constexpr (COMP) {
+                    R2 u = bnd[(p * nwarps + warp + 1) * NB + 2];
+                    ainlr = u.x; ainli = u.y;
+                }
+            } else {
+                ainr = 0; aini = 0; ainlr = 0; ainli = 0;
+            }
+        }
+        if (lane == 0) {
+            if (wa > 0) {
+                R2 t = bnd[(p * nwarps + warp - 1) * NB + 1];
+                binr = t.x; bini = t.y;
+                if constexpr (COMP) {
+                    R2 u = bnd[(p * nwarps + warp - 1) * NB + 3];
+                    binlr = u.x; binli = u.y;
+                }
+            } else {
+                binr = 0; bini = 0; binlr = 0; binli = 0;
+            }
+        }
+        const R2 *src = cs + (size_t)p * CPL * PS + L;
+        R pbr = binr, pbi = bini, pblr = binlr, pbli = binli;
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) {
+            const R ar = j + 1 < CPL ? Ar[j + 1] : ainr;
+            const R ai = j + 1 < CPL ? Ai[j + 1] : aini;
+            const R br = pbr, bi = pbi;
+            pbr = Br[j]; pbi = Bi[j];
+            const R2 e = src[j * PS];
+            const R m12r = k12r * e.x - k12i * e.y;
+            const R m12i = k12r * e.y + k12i * e.x;
+            const R m21r = k21r * e.x + k21i * e.y;
+            const R m21i = k21i * e.x - k21r * e.y;
+            if constexpr (!COMP) {
+                Ar[j] = fmaR(m12r, br, fmaR(-m12i, bi, ar));
+                Ai[j] = fmaR(m12r, bi, fmaR(m12i, br, ai));
+                Br[j] = fmaR(m21r, ar, fmaR(-m21i, ai, br));
+                Bi[j] = fmaR(m21r, ai, fmaR(m21i, ar, bi));
+            } else {
+                const R alr = j + 1 < CPL ? Alr[j + 1] : ainlr;
+                const R ali = j + 1 < CPL ? Ali[j + 1] : ainli;
+                const R blr = pblr, bli = pbli;
+                pblr = Blr[j]; pbli = Bli[j];
+                const R tr = fmaR(m12r, br, fmaR(-m12i, bi, alr));
+                const R ti = fmaR(m12r, bi, fmaR(m12i, br, ali));
+                const R ur = fmaR(m21r, ar, fmaR(-m21i, ai, blr));
+                const R ui = fmaR(m21r, ai, fmaR(m21i, ar, bli));
+                R e0, e1, e2, e3;
+                Ar[j] = two_sum(ar, tr, e0); Alr[j] = e0;
+                Ai[j] = two_sum(ai, ti, e1); Ali[j] = e1;
+                Br[j] = two_sum(br, ur, e2); Blr[j] = e2;
+                Bi[j] = two_sum(bi, ui, e3); Bli[j] = e3;
+            }
+        }
+        const int q = p ^ 1;
+        if (lane == 0) {
+            bnd[(q * nwarps + warp) * NB + 0] = R2{Ar[0], Ai[0]};
+            if constexpr (COMP) bnd[(q * nwarps + warp) * NB + 2] = R2{Alr[0], Ali[0]};
+        }
+        if (lane == 31) {
+            bnd[(q * nwarps + warp) * NB + 1] = R2{Br[CPL - 1], Bi[CPL - 1]};
+            if constexpr (COMP)
+                bnd[(q * nwarps + warp) * NB + 3] = R2{Blr[CPL - 1], Bli[CPL - 1]};
+        }
+        __syncthreads();
+    }
+
+    // ---------------------------------------------------------- output
+    if (ie_raw >= a.n_e) return;
+    const double2 S = __ldg(a.scale + ie);
+    R2 *out = reinterpret_cast<R2 *>(a.out) + ((size_t)ie * a.Ny + iy) * Nx;
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) {
+        const int x = L * CPL + j;
+        if (x < Nx) {
+            double br = (double)Br[j], bi = (double)Bi[j];
+            if constexpr (COMP) { br += (double)Blr[j]; bi += (double)Bli[j]; }
+            out[x] = R2{(R)(S.x * br - S.y * bi), (R)(S.x * bi + S.y * br)};
+        }
+    }
+}
+
+// Host launch of one instantiation; returns cudaError_t.  Also reports the
+// instantiation's maximum block size and register count.
+template <typename R, int CPL, int HT, bool COMP>
+cudaError_t launch_march(const MarchArgs &a, int grid, int block, size_t smem,
+                         cudaStream_t stream) {
+    auto *k = laue_march_kernel<R, CPL, HT, COMP>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k<<<grid, block, smem, stream>>>(a);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+template <typename R, int CPL, int HT, bool COMP>
+cudaError_t attr_march(cudaFuncAttributes *attr) {
+    return cudaFuncGetAttributes(attr, laue_march_kernel<R, CPL, HT, COMP>);
+}
+
+using MarchLaunch = cudaError_t (*)(const MarchArgs &, int, int, size_t,
+                                    cudaStream_t);
+using MarchAttr = cudaError_t (*)(cudaFuncAttributes *);
+
+struct MarchEntry {
+    MarchLaunch launch;
+    MarchAttr attr;
+};
+
+// Defined in laue_f64.cu / laue_f32.cu; return {nullptr, nullptr} for an
+// instantiation that does not exist.
+MarchEntry march_entry_f64(int cpl, int ht);
+MarchEntry march_entry_f32_plain(int cpl, int ht);
+MarchEntry march_entry_f32_comp(int cpl, int ht);
+extern const int kCplF64[];
+extern const int kNumCplF64;
+constexpr int kCplF32[] = {5, 7, 9, 11, 13};
+constexpr int kNumCplF32 = 5;
+
+}  // namespace dyfox

@@ -1,0 +1,76 @@
+// Diagnostics: the FMA-pipe throughput probe (roofline denominator of the
+// arithmetic-bound kernels) and the library's kernel-launch counter.
+#include <atomic>
+
+#include "common.cuh"
+
+namespace dyfox {
+
+std::atomic<unsigned long long> g_launches{0};
+
+void count_launch(unsigned n) { g_launches += n; }
+
+// Eight independent FMA chains per thread, `iters` rounds each.
+template <typename R>
+__global__ void fma_probe_kernel(R *out, int iters, R a, R b) {
+    R v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = (R)(threadIdx.x + i);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = v[i] * a + b;
+    }
+    R s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += v[i];
+    if (s == (R)-1.2345) out[0] = s;   // keeps the chains live
+}
+
+template <typename R>
+static int run_probe(int iters, double *tflops, cudaStream_t stream) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (!e) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e) return cuda_status(e, "probe device query");
+    R *out = nullptr;
+    cudaEvent_t t0, t1;
+    // The probe is a diagnostic outside the hot path: it owns its events
+    // and one scalar of device memory for the duration of the call.
+    if ((e = cudaMallocAsync((void **)&out, sizeof(R), stream)))
+        return cuda_status(e, "probe alloc");
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    const int blocks = sms * 8, threads = 256;
+    fma_probe_kernel<R><<<blocks, threads, 0, stream>>>(out, 64, (R)0.999, (R)1e-3);
+    cudaEventRecord(t0, stream);
+    fma_probe_kernel<R><<<blocks, threads, 0, stream>>>(out, iters, (R)0.999, (R)1e-3);
+    cudaEventRecord(t1, stream);
+    e = cudaEventSynchronize(t1);
+    float ms = 0;
+    if (!e) e = cudaEventElapsedTime(&ms, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaFreeAsync(out, stream);
+    if (e) return cuda_status(e, "probe timing");
+    double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return DYFOX_OK;
+}
+
+}  // namespace dyfox
+
+extern "C" int dyfox_pipe_peak(int precision, int iters, double *tflops,
+                               void *stream) {
+    dyfox::set_error("");
+    if (!tflops || iters < 1) {
+        dyfox::set_error("bad arguments to dyfox_pipe_peak");
+        return DYFOX_EINVAL;
+    }
+    if (precision == DYFOX_FP64)
+        return dyfox::run_probe<double>(iters, tflops, (cudaStream_t)stream);
+    return dyfox::run_probe<float>(iters, tflops, (cudaStream_t)stream);
+}
+
+extern "C" unsigned long long dyfox_launch_count(void) {
+    return dyfox::g_launches.load();
+}

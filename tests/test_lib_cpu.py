@@ -1,0 +1,131 @@
+"""The C-ABI library on the CPU: it loads, exports every entry point the
+header declares, and its host-only entry points and argument checks work
+without a GPU (no compute call is made here)."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+
+HEADER = os.path.join(ROOT, "include", "dyfox_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(dyfox_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from dyfox_gb300 import _lib, build
+    import shutil
+    if not os.path.exists(build.LIB):
+        if not shutil.which("nvcc") and not os.path.exists(
+                "/usr/local/cuda/bin/nvcc"):
+            pytest.skip("library not built and no nvcc")
+        build.build()
+    return _lib.lib()
+
+
+def test_header_declares_the_entry_points():
+    syms = declared_symbols()
+    for name in ("dyfox_laue_solve", "dyfox_h_grid", "dyfox_h_rows",
+                 "dyfox_segment_table", "dyfox_laue_workspace_bytes"):
+        assert name in syms
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_status_strings(lib):
+    from dyfox_gb300 import _lib
+    assert lib.dyfox_abi_version() == 1
+    assert lib.dyfox_status_string(_lib.DYFOX_EINVAL) == b"invalid argument"
+    assert lib.dyfox_status_string(99) == b"unknown status"
+
+
+def test_segment_table_matches_the_oracle_frames(lib, diamond400):
+    """dyfox_segment_table is host code: the frame equals the oracle's."""
+    from dyfox_gb300 import _lib
+    from oracle import oracle as O
+    v = golden("volterra")
+    for name in ("n", "x", "r", "screw", "zero"):
+        segs = [(s[:3], s[3:6], s[6:]) for s in v[f"segs_{name}"]]
+        t = _lib.segment_table(segs, diamond400.g_vec, diamond400.nu,
+                               diamond400.a_core, 0.25e-6)
+        f = O.segment_frames(segs, diamond400.g_vec)
+        np.testing.assert_allclose(t[:, :16], f, rtol=1e-15, atol=1e-30)
+
+
+def test_degenerate_segments_are_dropped(lib, diamond400):
+    from dyfox_gb300 import _lib
+    p = np.array([1e-6, 2e-6, 3e-6])
+    t = _lib.segment_table([(p, p, np.array([1e-10, 0, 0]))],
+                           diamond400.g_vec, diamond400.nu,
+                           diamond400.a_core, 0.25e-6)
+    assert len(t) == 0
+
+
+def test_non_finite_segment_is_rejected(lib, diamond400):
+    from dyfox_gb300 import _lib
+    bad = [(np.array([np.nan, 0, 0]), np.ones(3), np.ones(3))]
+    with pytest.raises(ValueError):
+        _lib.segment_table(bad, diamond400.g_vec, diamond400.nu,
+                           diamond400.a_core, 0.25e-6)
+
+
+def _desc(diamond400, small_grid, **kw):
+    from dyfox_gb300.grid import grid_arrays
+    from dyfox_gb300.laue import _desc
+    from dyfox_gb300.backend import FP64
+    d = _desc(diamond400, grid_arrays(small_grid), 3, FP64, 0)
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+def test_workspace_query_without_a_gpu(lib, diamond400, small_grid):
+    d = _desc(diamond400, small_grid)
+    n = lib.dyfox_laue_workspace_bytes(d)
+    assert n >= 3 * (small_grid.Nz - 1) * 32
+    assert lib.dyfox_laue_workspace_bytes(
+        _desc(diamond400, small_grid, Nz=1)) == 0
+    assert lib.dyfox_laue_workspace_bytes(
+        _desc(diamond400, small_grid, precision=7)) == 0
+
+
+@pytest.mark.parametrize("field,value,status", [
+    ("Nx", 0, 1), ("n_e", 0, 1), ("precision", 5, 1), ("h_source", 9, 1),
+    ("shift_px", -1.0, 1)])
+def test_bad_descriptors_fail_before_any_cuda_call(lib, diamond400,
+                                                   small_grid, field, value,
+                                                   status):
+    d = _desc(diamond400, small_grid, **{field: value})
+    st = lib.dyfox_laue_solve(d, ctypes.c_void_p(8), None, None,
+                              ctypes.c_void_p(8), None, 0, None)
+    assert st == status
+    assert lib.dyfox_last_error() != b""
+
+
+def test_null_pointers_are_rejected(lib, diamond400, small_grid):
+    d = _desc(diamond400, small_grid)
+    assert lib.dyfox_laue_solve(d, None, None, None, None, None, 0,
+                                None) == 1
+    st = lib.dyfox_laue_solve(d, ctypes.c_void_p(8), None, None,
+                              ctypes.c_void_p(8), None, 0, None)
+    assert st == 2          # workspace too small
+
+
+def test_solvers_fail_loudly_without_a_gpu(diamond400, small_grid):
+    from conftest import has_gpu
+    if has_gpu():
+        pytest.skip("a GPU is visible")
+    from dyfox_gb300.laue import solve_pristine
+    with pytest.raises(RuntimeError, match="CUDA"):
+        solve_pristine([0.0], small_grid, diamond400)
