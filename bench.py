@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--once", choices=["fp32", "fp64", "bragg"],
+                    help="run one solve of that form after one warm-up and "
+                         "exit (a small, fixed case for ncu)")
+    ap.add_argument("--no-bragg", action="store_true")
     return ap.parse_args()
 
 
@@ -70,6 +74,27 @@ def workload():
                            [-z0 * x.tan_tB, grid.dx / 2, z0], 800e-6)
     s = deviation_from_urad([0.0, 117.5], x)
     return x, grid, seg, s
+
+
+def bragg_workload():
+    """Bragg config 1: diamond (400) 17 keV, t = 20 um, dx = 0.5 um,
+    half_x = 16 um (Nz = 90, Nx = 456), 64 y-planes, 21 deviation parameters
+    evenly over +-3 Darwin widths, one edge dislocation (line [101],
+    b = (a/2)[10-1]) through the column at depth t/2, tol 1e-10."""
+    from dyfox_gb300.bragg_geometry import (BraggConfig, bragg_g_vector,
+                                            darwin_width_urad)
+    from dyfox_gb300.crystal import diamond_400
+    from dyfox_gb300.dislocations import burgers_vector, straight_segment
+    from dyfox_gb300.units import deviation_from_urad
+    x = diamond_400()
+    cfg = BraggConfig(x, t_crystal=20e-6, dx=0.5e-6, half_x=16e-6)
+    b = burgers_vector(np.eye(3), [1, 0, -1], x.b_mag, +1)
+    seg = straight_segment(np.array([1.0, 0.0, 1.0]) / np.sqrt(2.0), b,
+                           [0.0, 0.0, cfg.t_crystal / 2], 800e-6)
+    w = darwin_width_urad(x)
+    s = deviation_from_urad(np.linspace(-3 * w, 3 * w, 21), x)
+    ys = (np.arange(64) - 32 + 0.5) * cfg.dx
+    return x, cfg, seg, s, ys, bragg_g_vector(x)
 
 
 def active_rows(geo):
@@ -190,6 +215,20 @@ def run_ours(args):
 
     chosen, out32 = make(FP32)
     plain, out64 = make(FP64)
+    if args.once in ("fp32", "fp64"):
+        fn = chosen if args.once == "fp32" else plain
+        fn()
+        torch.cuda.synchronize()
+        fn()
+        torch.cuda.synchronize()
+        return
+    if args.once == "bragg":
+        from dyfox_gb300.bragg import solve_scan
+        bx, bcfg, bseg, bs, bys, bg = bragg_workload()
+        for _ in range(2):
+            solve_scan(bseg, bs[:4], bcfg, bys[:8], bx, bg)
+            torch.cuda.synchronize()
+        return
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def timed(fn, steps, warmup):
@@ -303,12 +342,66 @@ def run_ours(args):
     }
     clk_sum = clk.summary()
     line["clocks"] = clk_sum
+    if not args.no_bragg:
+        line["bragg"] = bragg_leg(args, rank, world)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, grid, seg, s, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def bragg_leg(args, rank, world):
+    """Bragg solves/s of config 1: all 21 deviation parameters x 64 planes
+    in one batched launch (one solve = one deviation parameter over all
+    planes, to true relative residual <= 1e-10), plain FP64."""
+    import torch
+    from dyfox_gb300 import _lib
+    from dyfox_gb300.bragg import solve_scan
+    x, cfg, seg, s, ys, g = bragg_workload()
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(2):
+        out, info = solve_scan(seg, s, cfg, ys, x, g)
+    torch.cuda.synchronize()
+    steps = max(3, args.steps // 4)
+    times = []
+    n0 = L.dyfox_launch_count()
+    for _ in range(steps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out, info = solve_scan(seg, s, cfg, ys, x, g)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    launches = L.dyfox_launch_count() - n0
+    inf = info.cpu().numpy()
+    ms = statistics.mean(times)
+    res = {"value": world * len(s) / (ms * 1e-3), "unit": "Bragg solves/s",
+           "ms_per_scan": ms, "solves_per_scan": len(s),
+           "planes": len(ys), "Nx": cfg.Nx, "Nz": cfg.Nz,
+           "form": "plain FP64, per-plane GMRES(40), one launch per scan",
+           "max_true_residual": float(inf[:, 0].max()),
+           "max_inner_iterations": int(inf[:, 1].max()),
+           "converged": bool((inf[:, 0] <= 1e-10).all()),
+           "gpu_launches": int(launches)}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import bragg_oracle as BO
+        t0 = time.perf_counter()
+        _, cinfo = BO.solve_surface(seg, float(s[len(s) // 2]), cfg, ys, x,
+                                    g)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {
+            "value": 1.0 / dt, "unit": "Bragg solves/s", "cores": 1,
+            "kind": "port", "sample": "1 of 21 deviation parameters, 64 "
+            "planes (the reference's chunked SciPy GMRES restated in "
+            f"NumPy; NumPy elementwise and FFT are single-threaded), "
+            f"{dt:.1f} s, {cinfo['iterations']} iterations"}
+    return res
 
 
 # ------------------------------------------------------------- CPU legs

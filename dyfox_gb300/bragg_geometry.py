@@ -83,3 +83,12 @@ def threading_segment(kind, sign, b_mag, g_mag, psi=np.pi / 4, y0=0.0,
     core = np.array([x0, y0, 0.0])
     half = 300e-6
     return [(core - half * xi, core + half * xi, bv)]
+
+
+def darwin_width_urad(xtal):
+    """Full width (urad) of the symmetric-Bragg total-reflection domain:
+    2 |sqrt(chi_h chi_hbar)| / sin(2 theta_B), with chi = lambda sigma /
+    (i pi) (DYFOX bragg/reference.py:59-67)."""
+    sh, sb = complex(xtal.sig_h), complex(xtal.sig_hbar)
+    chi = np.sqrt(sh * sb) * xtal.lam / (1j * np.pi)
+    return float(2.0 * abs(chi) / xtal.sin_2tB * 1e6)

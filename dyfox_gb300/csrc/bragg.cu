@@ -1,0 +1,726 @@
+// Bragg (reflection) shooting solve: couplings, the perfect-crystal
+// symbol, and one persistent GMRES per system (y-plane x deviation
+// parameter), replacing DYFOX bragg/solver.py:28-60 and 135-379.
+//
+// Shooting form (bragg/solver.py:1-20): march D0, Dg down from z = 0 with
+// D_g(0) = v unknown; the back-face condition D_g(t) = 0 gives A v = -d,
+// A v = march(0, v), d = march(incident, 0).  Each system is solved with
+// restarted GMRES, left-preconditioned by M w = ifft(fft(w) / T22s), in the
+// published algorithm of SciPy 1.18's scipy.sparse.linalg.gmres (modified
+// Gram-Schmidt Arnoldi, Givens rotations (LAPACK lartg), adaptive inner
+// tolerance, true residual at every restart).  The exit wave is
+// v e^{-iH(z=0)}.
+#include <math.h>
+#include <string.h>
+
+#include "bragg.cuh"
+#include "volterra.cuh"
+
+namespace dyfox {
+
+struct BraggArgs {
+    int Nx, Nz, n_y, n_s;
+    double ds, s0r, s0i, shr, shi, sbr, sbi;
+    const double *s_dev;          // (n_s)
+    const double2 *cb, *ch;       // (n_y, Nz, Nx): ds sigma e^{+-iH}
+    const double2 *e0h;           // (n_y, Nx): e^{-iH(z=0)}
+    const double2 *inc;           // (Nx): incident D0
+    const double2 *iT;            // (n_s, Nx): 1 / T22s
+    const double2 *tw;            // (Nx): exp(-2 pi i m / Nx)
+    FftPlan plan;
+    double2 *V;                   // (n_sys, m + 1, Nx)
+    double2 *Hh;                  // (n_sys, m, m + 1)
+    double2 *X, *B;               // (n_sys, Nx)
+    double2 *out;                 // (n_s, n_y, Nx)
+    double *info;                 // (n_sys, 4)
+    double tol;
+    int restart, maxiter, use_x0;
+};
+
+__device__ __forceinline__ void step_factors(const BraggArgs &a, int is,
+                                             double2 &e0, double2 &ieg) {
+    const double alpha = -2.0 * kPi * a.s_dev[is];
+    const double er = exp(a.s0r * a.ds);
+    double sn, c;
+    sincos(a.s0i * a.ds, &sn, &c);
+    e0 = make_double2(er * c, er * sn);
+    sincos((a.s0i + alpha) * a.ds, &sn, &c);
+    // 1 / eg = exp(-(s0 + i alpha) ds)
+    ieg = make_double2(c / er, -sn / er);
+}
+
+// Couplings of every plane: cb = ds (sigma_hbar e^{+iH}), ch = ds (sigma_h
+// e^{-iH}) with H the Volterra phase at (x_i, y_p, z_k) summed in segment
+// order; e0h = e^{-iH} at k = 0.  One thread per voxel.
+__global__ void bragg_couple_kernel(const double *__restrict__ segs,
+                                    int n_seg, int Nx, int Nz, double dx,
+                                    double dz, VolterraConsts vc,
+                                    const double *__restrict__ y, int n_y,
+                                    double ds, double shr, double shi,
+                                    double sbr, double sbi, double2 *cb,
+                                    double2 *ch, double2 *e0h) {
+    const long total = (long)n_y * Nz * Nx;
+    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long)gridDim.x * blockDim.x) {
+        const int x = (int)(idx % Nx);
+        const long t = idx / Nx;
+        const int k = (int)(t % Nz);
+        const int p = (int)(t / Nz);
+        const double X0 = __dmul_rn((double)x - 0.5 * Nx, dx);
+        const double zv = __dmul_rn((double)k, dz);
+        double H = 0.0;
+        for (int s = 0; s < n_seg; ++s) {
+            const double *sg = segs + (size_t)s * DYFOX_SEG_STRIDE;
+            H = __dadd_rn(H, h_seg_f64(sg, __dsub_rn(X0, __ldg(sg + SEG_CX)),
+                                       __dsub_rn(y[p], __ldg(sg + SEG_CY)),
+                                       __dsub_rn(zv, __ldg(sg + SEG_CZ)), vc));
+        }
+        double sn, c;
+        sincos(H, &sn, &c);
+        // sigma e^{-+iH}, then ds times each part (solver.py:260-261, 31-32)
+        const double2 a = make_double2(shr * c + shi * sn, shi * c - shr * sn);
+        const double2 b = make_double2(sbr * c - sbi * sn, sbi * c + sbr * sn);
+        cb[idx] = make_double2(ds * b.x, ds * b.y);
+        ch[idx] = make_double2(ds * a.x, ds * a.y);
+        if (k == 0) e0h[(size_t)p * Nx + x] = make_double2(c, -sn);
+    }
+}
+
+// exp(-2 pi i m / N) for m in [0, N).
+__global__ void twiddle_kernel(double2 *tw, int N) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= N) return;
+    double sn, c;
+    sincospi(-2.0 * m / N, &sn, &c);
+    tw[m] = make_double2(c, sn);
+}
+
+// perfect_symbol (bragg/solver.py:38-60): per Fourier mode the 2 x 2 chain
+// of the unstrained down-march; T22 floored at 1e-8 max|T22| (164-165,
+// 277-278) and inverted into iT.  One CTA per deviation parameter.
+__global__ void bragg_symbol_kernel(const double *__restrict__ s_dev, int Nx,
+                                    int Nz, double ds, double s0r, double s0i,
+                                    double shr, double shi, double sbr,
+                                    double sbi, double2 *T21, double2 *T22,
+                                    double2 *iT) {
+    __shared__ double2 red[33];
+    const int is = blockIdx.x;
+    const double alpha = -2.0 * kPi * s_dev[is];
+    const double er = exp(s0r * ds);
+    double sn, c;
+    sincos(s0i * ds, &sn, &c);
+    const double2 e0 = make_double2(er * c, er * sn);
+    sincos((s0i + alpha) * ds, &sn, &c);
+    const double2 eg = make_double2(er * c, er * sn);
+    const double2 ieg = make_double2(c / er, -sn / er);
+    const double2 sh = make_double2(shr, shi), sb = make_double2(sbr, sbi);
+    double mx = 0.0;
+    for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
+        // fftfreq: m = x for x < ceil(N/2), else x - N
+        const int m = x < (Nx + 1) / 2 ? x : x - Nx;
+        double ps, pc;
+        sincospi(-2.0 * m / Nx, &ps, &pc);
+        const double2 p = make_double2(pc, ps), pi = make_double2(pc, -ps);
+        const double2 a11 = cmulz(e0, p);
+        const double2 a12 = cmulz(cscale(ds, a11), sb);
+        const double2 a21 = cmulz(cmulz(cscale(-ds, pi), sh), ieg);
+        const double2 a22 = cmulz(pi, ieg);
+        double2 t11 = make_double2(1, 0), t12 = make_double2(0, 0);
+        double2 t21 = make_double2(0, 0), t22 = make_double2(1, 0);
+        for (int k = 0; k < Nz - 1; ++k) {
+            const double2 n11 = cadd(cmulz(a11, t11), cmulz(a12, t21));
+            const double2 n12 = cadd(cmulz(a11, t12), cmulz(a12, t22));
+            const double2 n21 = cadd(cmulz(a21, t11), cmulz(a22, t21));
+            const double2 n22 = cadd(cmulz(a21, t12), cmulz(a22, t22));
+            t11 = n11; t12 = n12; t21 = n21; t22 = n22;
+        }
+        if (T21) T21[(size_t)is * Nx + x] = t21;
+        if (T22) T22[(size_t)is * Nx + x] = t22;
+        if (iT) iT[(size_t)is * Nx + x] = t22;
+        mx = fmax(mx, hypot(t22.x, t22.y));
+    }
+    (void)eg;
+    if (!iT) return;
+    const double floor_ = 1e-8 * block_max(mx, red);
+    for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
+        double2 t = iT[(size_t)is * Nx + x];
+        if (hypot(t.x, t.y) < floor_) t = make_double2(floor_, 0.0);
+        const double d = t.x * t.x + t.y * t.y;
+        iT[(size_t)is * Nx + x] = make_double2(t.x / d, -t.y / d);
+    }
+}
+
+// Shared memory of the GMRES kernel: three Nx rows (exchange / FFT scratch
+// and the Arnoldi vector), the reduction slots, S, y and the rotations.
+__host__ __device__ inline size_t gmres_smem(int Nx, int m) {
+    return (size_t)3 * Nx * sizeof(double2) + 34 * sizeof(double2) +
+           (size_t)2 * (m + 1) * sizeof(double2) +
+           (size_t)m * (sizeof(double2) + sizeof(double)) + 64;
+}
+
+// LAPACK zlartg: c real, s complex, r with [c s; -conj(s) c] [f; g] = [r; 0].
+__device__ void lartg(double2 f, double2 g, double &c, double2 &s,
+                      double2 &r) {
+    const double fa = hypot(f.x, f.y), ga = hypot(g.x, g.y);
+    if (ga == 0.0) {
+        c = 1.0; s = make_double2(0.0, 0.0); r = f;
+    } else if (fa == 0.0) {
+        c = 0.0; s = make_double2(g.x / ga, -g.y / ga); r = make_double2(ga, 0.0);
+    } else {
+        const double d = hypot(fa, ga);
+        c = fa / d;
+        const double2 fu = make_double2(f.x / fa, f.y / fa);   // f / |f|
+        s = cscale(1.0 / d, cmulz(fu, cconj(g)));
+        r = cscale(d, fu);
+    }
+}
+
+template <int CPL>
+__global__ void bragg_gmres_kernel(const BraggArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int Nx = a.Nx, m = a.restart;
+    double2 *A0 = reinterpret_cast<double2 *>(smem);
+    double2 *A1 = A0 + Nx;
+    double2 *W = A1 + Nx;
+    double2 *red = W + Nx;     // [0, 33): block_sum; [33]: presid
+    double2 *S = red + 34;
+    double2 *yv = S + (m + 1);
+    double2 *gs = yv + (m + 1);
+    double *gc = reinterpret_cast<double *>(gs + m);
+    int *flags = reinterpret_cast<int *>(gc + m);          // [0] stop
+
+    const int sys = blockIdx.x, is = sys / a.n_y, iy = sys - is * a.n_y;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const double2 *cb = a.cb + (size_t)iy * a.Nz * Nx;
+    const double2 *ch = a.ch + (size_t)iy * a.Nz * Nx;
+    const double2 *iT = a.iT + (size_t)is * Nx;
+    double2 *V = a.V + (size_t)sys * (m + 1) * Nx;
+    double2 *Hh = a.Hh + (size_t)sys * m * (m + 1);
+    double2 *X = a.X + (size_t)sys * Nx;
+    double2 *B = a.B + (size_t)sys * Nx;
+    double2 e0, ieg;
+    step_factors(a, is, e0, ieg);
+    const double eps = 2.220446049250313e-16;
+
+    auto norm2 = [&](const double2 *v) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int x = tid; x < Nx; x += nt) t.x += cabs2(v[x]);
+        return sqrt(block_sum(t, red).x);
+    };
+    // W <- A src (src NULL: particular solution from the incident beam)
+    auto matvec = [&](const double2 *src) {
+        if (src) bragg_march<CPL>(cb, ch, e0, ieg, a.Nz, Nx, nullptr, src,
+                                  A0, A1, W);
+        else bragg_march<CPL>(cb, ch, e0, ieg, a.Nz, Nx, a.inc, nullptr, A0,
+                              A1, W);
+    };
+
+    // b = -d
+    matvec(nullptr);
+    for (int x = tid; x < Nx; x += nt) {
+        B[x] = make_double2(-W[x].x, -W[x].y);
+        if (!a.use_x0) X[x] = make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    const double bnrm2 = norm2(B);
+    double *info = a.info + (size_t)sys * 4;
+    double rnorm = 0.0;
+    int inner = 0, code = 0;
+    if (bnrm2 == 0.0) {
+        for (int x = tid; x < Nx; x += nt) X[x] = make_double2(0.0, 0.0);
+    } else {
+        const double atol = a.tol * bnrm2;
+        for (int x = tid; x < Nx; x += nt) W[x] = B[x];
+        __syncthreads();
+        precond_apply(W, A0, A1, a.plan, a.tw, iT);
+        const double Mb_nrm2 = norm2(W);
+        double ptol_max_factor = 1.0;
+        double ptol = Mb_nrm2 * fmin(ptol_max_factor, atol / bnrm2);
+        double presid = 0.0;
+        // r = b - A x0 (b when x0 is zero)
+        bool nonzero = false;
+        if (a.use_x0) {
+            double2 t = make_double2(0.0, 0.0);
+            for (int x = tid; x < Nx; x += nt) t.x += cabs2(X[x]);
+            nonzero = block_sum(t, red).x > 0.0;
+        }
+        if (nonzero) {
+            matvec(X);
+            for (int x = tid; x < Nx; x += nt) W[x] = csub(B[x], W[x]);
+        } else {
+            for (int x = tid; x < Nx; x += nt) W[x] = B[x];
+        }
+        __syncthreads();
+        rnorm = norm2(W);
+        code = a.maxiter;
+        if (rnorm < atol) {
+            code = 0;
+        } else {
+            for (int iter = 0; iter < a.maxiter; ++iter) {
+                // v0 = M r / |M r|, S = (|M r|, 0, ...)
+                precond_apply(W, A0, A1, a.plan, a.tw, iT);
+                const double tmp = norm2(W);
+                for (int x = tid; x < Nx; x += nt) V[x] = cscale(1.0 / tmp, W[x]);
+                for (int j = tid; j <= m; j += nt)
+                    S[j] = make_double2(j == 0 ? tmp : 0.0, 0.0);
+                __syncthreads();
+                bool breakdown = false;
+                int col = 0;
+                for (col = 0; col < m; ++col) {
+                    matvec(V + (size_t)col * Nx);
+                    precond_apply(W, A0, A1, a.plan, a.tw, iT);
+                    const double h0 = norm2(W);
+                    // Modified Gram-Schmidt, one pass per basis vector:
+                    // subtract the previous projection, accumulate the next.
+                    double2 hprev = make_double2(0.0, 0.0);
+                    for (int k = 0; k <= col; ++k) {
+                        const double2 *vk = V + (size_t)k * Nx;
+                        const double2 *vp = k ? V + (size_t)(k - 1) * Nx : vk;
+                        double2 t = make_double2(0.0, 0.0);
+                        for (int x = tid; x < Nx; x += nt) {
+                            double2 w = W[x];
+                            if (k) w = csub(w, cmulz(hprev, vp[x]));
+                            W[x] = w;
+                            const double2 d = cdotz(vk[x], w);
+                            t.x += d.x;
+                            t.y += d.y;
+                        }
+                        const double2 h = block_sum(t, red);
+                        if (tid == 0) Hh[(size_t)col * (m + 1) + k] = h;
+                        hprev = h;
+                    }
+                    {
+                        const double2 *vp = V + (size_t)col * Nx;
+                        for (int x = tid; x < Nx; x += nt)
+                            W[x] = csub(W[x], cmulz(hprev, vp[x]));
+                    }
+                    __syncthreads();
+                    const double h1 = norm2(W);
+                    double2 *vn = V + (size_t)(col + 1) * Nx;
+                    if (h1 <= eps * h0) {
+                        breakdown = true;
+                        for (int x = tid; x < Nx; x += nt) vn[x] = W[x];
+                    } else {
+                        for (int x = tid; x < Nx; x += nt)
+                            vn[x] = cscale(1.0 / h1, W[x]);
+                    }
+                    if (tid == 0) {
+                        double2 *hc = Hh + (size_t)col * (m + 1);
+                        hc[col + 1] = make_double2(breakdown ? 0.0 : h1, 0.0);
+                        for (int k = 0; k < col; ++k) {
+                            const double c = gc[k];
+                            const double2 s = gs[k];
+                            const double2 n0 = hc[k], n1 = hc[k + 1];
+                            hc[k] = cadd(cscale(c, n0), cmulz(s, n1));
+                            hc[k + 1] = cadd(cscale(-1.0, cmulz(cconj(s), n0)),
+                                             cscale(c, n1));
+                        }
+                        double c;
+                        double2 s, r;
+                        lartg(hc[col], hc[col + 1], c, s, r);
+                        gc[col] = c;
+                        gs[col] = s;
+                        hc[col] = r;
+                        hc[col + 1] = make_double2(0.0, 0.0);
+                        const double2 t = cscale(-1.0, cmulz(cconj(s), S[col]));
+                        S[col] = cscale(c, S[col]);
+                        S[col + 1] = t;
+                        red[33].x = hypot(t.x, t.y);
+                    }
+                    __syncthreads();
+                    presid = red[33].x;
+                    ++inner;
+                    __syncthreads();
+                    if (presid <= ptol || breakdown) break;
+                }
+                if (col == m) col = m - 1;
+                // y = R^{-1} S (back substitution; R[row][c] = Hh[c][row])
+                if (tid == 0) {
+                    const double2 *Hc = Hh;
+                    if (Hc[(size_t)col * (m + 1) + col].x == 0.0 &&
+                        Hc[(size_t)col * (m + 1) + col].y == 0.0)
+                        S[col] = make_double2(0.0, 0.0);
+                    for (int k = 0; k <= col; ++k) yv[k] = S[k];
+                    for (int k = col; k > 0; --k) {
+                        if (yv[k].x != 0.0 || yv[k].y != 0.0) {
+                            const double2 hkk = Hc[(size_t)k * (m + 1) + k];
+                            const double d = cabs2(hkk);
+                            yv[k] = cscale(1.0 / d, cmulz(yv[k], cconj(hkk)));
+                            const double2 tk = yv[k];
+                            for (int i = 0; i < k; ++i)
+                                yv[i] = csub(yv[i],
+                                             cmulz(tk, Hc[(size_t)k * (m + 1) + i]));
+                        }
+                    }
+                    if (yv[0].x != 0.0 || yv[0].y != 0.0) {
+                        const double2 h00 = Hc[0];
+                        yv[0] = cscale(1.0 / cabs2(h00), cmulz(yv[0], cconj(h00)));
+                    }
+                }
+                __syncthreads();
+                for (int x = tid; x < Nx; x += nt) {
+                    double2 acc = X[x];
+                    for (int k = 0; k <= col; ++k)
+                        acc = cadd(acc, cmulz(yv[k], V[(size_t)k * Nx + x]));
+                    X[x] = acc;
+                }
+                __syncthreads();
+                matvec(X);
+                for (int x = tid; x < Nx; x += nt) W[x] = csub(B[x], W[x]);
+                __syncthreads();
+                rnorm = norm2(W);
+                if (rnorm <= atol) { code = 0; break; }
+                if (breakdown) break;
+                if (presid <= ptol)
+                    ptol_max_factor = fmax(eps, 0.25 * ptol_max_factor);
+                else
+                    ptol_max_factor = fmin(1.0, 1.5 * ptol_max_factor);
+                ptol = presid * fmin(ptol_max_factor, atol / rnorm);
+            }
+            if (rnorm <= atol) code = 0;
+        }
+    }
+    // exit wave v e^{-iH(0)}
+    double2 *out = a.out + ((size_t)is * a.n_y + iy) * Nx;
+    const double2 *e0h = a.e0h + (size_t)iy * Nx;
+    for (int x = tid; x < Nx; x += nt) out[x] = cmulz(X[x], __ldg(e0h + x));
+    if (tid == 0) {
+        info[0] = bnrm2 > 0.0 ? rnorm / bnrm2 : 0.0;
+        info[1] = inner;
+        info[2] = code;
+        info[3] = bnrm2;
+    }
+    (void)flags;
+}
+
+// Matvec / preconditioner for parity checks: one CTA per system.
+// mode 0: out = march(d0, dg); mode 1: out = M in.
+template <int CPL>
+__global__ void bragg_apply_kernel(const BraggArgs a, int mode,
+                                   const double2 *d0, const double2 *dg,
+                                   double2 *out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int Nx = a.Nx;
+    double2 *A0 = reinterpret_cast<double2 *>(smem);
+    double2 *A1 = A0 + Nx;
+    double2 *W = A1 + Nx;
+    const int sys = blockIdx.x, is = sys / a.n_y, iy = sys - is * a.n_y;
+    const size_t off = (size_t)sys * Nx;
+    if (mode == 0) {
+        double2 e0, ieg;
+        step_factors(a, is, e0, ieg);
+        bragg_march<CPL>(a.cb + (size_t)iy * a.Nz * Nx,
+                         a.ch + (size_t)iy * a.Nz * Nx, e0, ieg, a.Nz, Nx,
+                         d0 ? d0 + off : nullptr, dg ? dg + off : nullptr, A0,
+                         A1, W);
+    } else {
+        for (int x = threadIdx.x; x < Nx; x += blockDim.x) W[x] = d0[off + x];
+        __syncthreads();
+        precond_apply(W, A0, A1, a.plan, a.tw, a.iT + (size_t)is * Nx);
+    }
+    for (int x = threadIdx.x; x < Nx; x += blockDim.x) out[off + x] = W[x];
+}
+
+// ---------------------------------------------------------------------------
+static FftPlan make_fft_plan(int N) {
+    FftPlan p;
+    memset(&p, 0, sizeof p);
+    p.n = N;
+    int n = N;
+    while (n % 4 == 0 && p.nfac < 24) { p.fac[p.nfac++] = 4; n /= 4; }
+    while (n % 2 == 0 && p.nfac < 24) { p.fac[p.nfac++] = 2; n /= 2; }
+    for (int f = 3; n > 1 && p.nfac < 24; f += 2)
+        while (n % f == 0 && p.nfac < 24) { p.fac[p.nfac++] = f; n /= f; }
+    return p;
+}
+
+struct BraggPlan {
+    int threads, cpl;
+    size_t off_cb, off_ch, off_e0h, off_inc, off_iT, off_tw, off_y;
+    size_t off_V, off_H, off_X, off_B, off_info, ws;
+};
+
+static size_t a256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static int bragg_validate(const dyfox_bragg_desc *d) {
+    if (!d) { set_error("descriptor is NULL"); return DYFOX_EINVAL; }
+    if (d->Nx < 2 || d->Nz < 2 || d->n_y < 1 || d->n_s < 1 || d->n_seg < 0) {
+        set_error("bad sizes Nx=%d Nz=%d n_y=%d n_s=%d n_seg=%d", d->Nx, d->Nz,
+                  d->n_y, d->n_s, d->n_seg);
+        return DYFOX_EINVAL;
+    }
+    if (d->Nx > 16 * 512) {
+        set_error("Nx=%d above the supported 8192", d->Nx);
+        return DYFOX_ENOSYS;
+    }
+    if (!(d->ds > 0) || !(d->dx > 0) || !(d->dz > 0) || !(d->tol > 0) ||
+        d->restart < 1 || d->maxiter < 1 || d->restart > 1024) {
+        set_error("bad scalars ds=%g dx=%g dz=%g tol=%g restart=%d maxiter=%d",
+                  d->ds, d->dx, d->dz, d->tol, d->restart, d->maxiter);
+        return DYFOX_EINVAL;
+    }
+    if (d->precision != DYFOX_FP64) {
+        set_error("the Bragg solve runs in DYFOX_FP64");
+        return DYFOX_ENOSYS;
+    }
+    return DYFOX_OK;
+}
+
+static int bragg_plan(const dyfox_bragg_desc *d, BraggPlan *p) {
+    int st = bragg_validate(d);
+    if (st) return st;
+    const size_t Nx = d->Nx, plane = (size_t)d->Nz * Nx * sizeof(double2);
+    const size_t nsys = (size_t)d->n_y * d->n_s;
+    const int m = d->restart;
+    // Columns per thread of the march: a power of two <= 8 for Nx <= 4096.
+    p->threads = Nx <= 512 ? 128 : (Nx <= 2048 ? 256 : 512);
+    p->cpl = (int)((Nx + p->threads - 1) / p->threads);
+    int c = 1;
+    while (c < p->cpl) c *= 2;
+    p->cpl = c;
+    size_t o = 0;
+    p->off_cb = o; o = a256(o + d->n_y * plane);
+    p->off_ch = o; o = a256(o + d->n_y * plane);
+    p->off_e0h = o; o = a256(o + d->n_y * Nx * sizeof(double2));
+    p->off_inc = o; o = a256(o + Nx * sizeof(double2));
+    p->off_iT = o; o = a256(o + d->n_s * Nx * sizeof(double2));
+    p->off_tw = o; o = a256(o + Nx * sizeof(double2));
+    p->off_y = o; o = a256(o + d->n_y * sizeof(double));
+    p->off_V = o; o = a256(o + nsys * (m + 1) * Nx * sizeof(double2));
+    p->off_H = o; o = a256(o + nsys * m * (m + 1) * sizeof(double2));
+    p->off_X = o; o = a256(o + nsys * Nx * sizeof(double2));
+    p->off_B = o; o = a256(o + nsys * Nx * sizeof(double2));
+    p->off_info = o; o = a256(o + nsys * 4 * sizeof(double));
+    p->ws = o;
+    return DYFOX_OK;
+}
+
+__global__ void incident_kernel(double2 *inc, int Nx, double dx, int beam,
+                                double thickness, double centre) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= Nx) return;
+    double v = 1.0;
+    if (beam) {
+        const double xp = (x - Nx / 2.0) * dx;
+        v = fabs(xp - centre) < 0.5 * thickness ? 1.0 : 0.0;
+    }
+    inc[x] = make_double2(v, 0.0);
+}
+
+// Couplings, incident beam, twiddles and the preconditioner for `d`.
+static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
+                         const double *seg_table, const double *y_host,
+                         const double *s_dev, char *ws, cudaStream_t stream,
+                         BraggArgs *a) {
+    memset(a, 0, sizeof *a);
+    a->Nx = d->Nx; a->Nz = d->Nz; a->n_y = d->n_y; a->n_s = d->n_s;
+    a->ds = d->ds;
+    a->s0r = d->sig0[0]; a->s0i = d->sig0[1];
+    a->shr = d->sig_h[0]; a->shi = d->sig_h[1];
+    a->sbr = d->sig_hbar[0]; a->sbi = d->sig_hbar[1];
+    a->s_dev = s_dev;
+    a->cb = (double2 *)(ws + p.off_cb);
+    a->ch = (double2 *)(ws + p.off_ch);
+    a->e0h = (double2 *)(ws + p.off_e0h);
+    a->inc = (double2 *)(ws + p.off_inc);
+    a->iT = (double2 *)(ws + p.off_iT);
+    a->tw = (double2 *)(ws + p.off_tw);
+    a->plan = make_fft_plan(d->Nx);
+    a->V = (double2 *)(ws + p.off_V);
+    a->Hh = (double2 *)(ws + p.off_H);
+    a->X = (double2 *)(ws + p.off_X);
+    a->B = (double2 *)(ws + p.off_B);
+    a->info = (double *)(ws + p.off_info);
+    a->tol = d->tol;
+    a->restart = d->restart;
+    a->maxiter = d->maxiter;
+    cudaError_t e;
+    double *y = (double *)(ws + p.off_y);
+    if ((e = cudaMemcpyAsync(y, y_host, sizeof(double) * d->n_y,
+                             cudaMemcpyHostToDevice, stream)))
+        return cuda_status(e, "y upload");
+    const long total = (long)d->n_y * d->Nz * d->Nx;
+    long blocks = (total + 255) / 256;
+    if (blocks > 152L * 64) blocks = 152L * 64;
+    bragg_couple_kernel<<<(int)blocks, 256, 0, stream>>>(
+        seg_table, d->n_seg, d->Nx, d->Nz, d->dx, d->dz,
+        volterra_consts(d->nu, d->a_core), y, d->n_y, d->ds, a->shr, a->shi,
+        a->sbr, a->sbi, (double2 *)a->cb, (double2 *)a->ch, (double2 *)a->e0h);
+    incident_kernel<<<div_up(d->Nx, 256), 256, 0, stream>>>(
+        (double2 *)a->inc, d->Nx, d->dx, d->beam, d->beam_thickness,
+        d->beam_centre);
+    twiddle_kernel<<<div_up(d->Nx, 256), 256, 0, stream>>>((double2 *)a->tw,
+                                                           d->Nx);
+    bragg_symbol_kernel<<<d->n_s, 256, 0, stream>>>(
+        s_dev, d->Nx, d->Nz, d->ds, a->s0r, a->s0i, a->shr, a->shi, a->sbr,
+        a->sbi, nullptr, nullptr, (double2 *)a->iT);
+    count_launch(4);
+    return cuda_status(cudaGetLastError(), "bragg prepare");
+}
+
+template <int CPL>
+static cudaError_t launch_gmres(const BraggArgs &a, int threads, size_t smem,
+                                int grid, cudaStream_t stream) {
+    auto *k = bragg_gmres_kernel<CPL>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e) return e;
+    }
+    k<<<grid, threads, smem, stream>>>(a);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+template <int CPL>
+static cudaError_t launch_apply(const BraggArgs &a, int threads, size_t smem,
+                                int grid, int mode, const double2 *d0,
+                                const double2 *dg, double2 *out,
+                                cudaStream_t stream) {
+    auto *k = bragg_apply_kernel<CPL>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e) return e;
+    }
+    k<<<grid, threads, smem, stream>>>(a, mode, d0, dg, out);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+static int smem_ok(size_t need) {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (!e) e = cudaDeviceGetAttribute(&optin,
+                                       cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e) return cuda_status(e, "device query");
+    if (need > (size_t)optin) {
+        set_error("Bragg kernel needs %zu bytes of shared memory, the device "
+                  "allows %d", need, optin);
+        return DYFOX_ESMEM;
+    }
+    return DYFOX_OK;
+}
+
+}  // namespace dyfox
+
+using namespace dyfox;
+
+extern "C" size_t dyfox_bragg_workspace_bytes(const dyfox_bragg_desc *d) {
+    BraggPlan p;
+    if (bragg_plan(d, &p)) return 0;
+    return p.ws;
+}
+
+extern "C" int dyfox_bragg_solve(const dyfox_bragg_desc *d,
+                                 const double *seg_table,
+                                 const double *y_values, const double *s_dev,
+                                 const void *x0, void *out, double *info,
+                                 void *workspace, size_t workspace_bytes,
+                                 void *stream_) {
+    set_error("");
+    BraggPlan p;
+    int st = bragg_plan(d, &p);
+    if (st) return st;
+    if (!y_values || !s_dev || !out || (d->n_seg > 0 && !seg_table)) {
+        set_error("NULL argument to dyfox_bragg_solve");
+        return DYFOX_EINVAL;
+    }
+    if (workspace_bytes < p.ws || !workspace) {
+        set_error("workspace of %zu bytes, %zu needed", workspace_bytes, p.ws);
+        return DYFOX_ENOMEM;
+    }
+    const size_t smem = gmres_smem(d->Nx, d->restart);
+    if ((st = smem_ok(smem))) return st;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    char *ws = (char *)workspace;
+    BraggArgs a;
+    if ((st = bragg_prepare(d, p, seg_table, y_values, s_dev, ws, stream, &a)))
+        return st;
+    const size_t nsys = (size_t)d->n_y * d->n_s;
+    cudaError_t e;
+    if (x0) {
+        if ((e = cudaMemcpyAsync(a.X, x0, nsys * d->Nx * sizeof(double2),
+                                 cudaMemcpyDeviceToDevice, stream)))
+            return cuda_status(e, "x0 copy");
+        a.use_x0 = 1;
+    }
+    a.out = (double2 *)out;
+    const int g = (int)nsys;
+    switch (p.cpl) {
+    case 1: e = launch_gmres<1>(a, p.threads, smem, g, stream); break;
+    case 2: e = launch_gmres<2>(a, p.threads, smem, g, stream); break;
+    case 4: e = launch_gmres<4>(a, p.threads, smem, g, stream); break;
+    case 8: e = launch_gmres<8>(a, p.threads, smem, g, stream); break;
+    default: e = launch_gmres<16>(a, p.threads, smem, g, stream); break;
+    }
+    if (e) return cuda_status(e, "bragg_gmres");
+    if (info) {
+        if ((e = cudaMemcpyAsync(info, a.info, nsys * 4 * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, stream)))
+            return cuda_status(e, "info copy");
+    }
+    return DYFOX_OK;
+}
+
+extern "C" int dyfox_bragg_apply(const dyfox_bragg_desc *d, int mode,
+                                 const double *seg_table,
+                                 const double *y_values, const double *s_dev,
+                                 const void *in0, const void *in1, void *out,
+                                 void *workspace, size_t workspace_bytes,
+                                 void *stream_) {
+    set_error("");
+    BraggPlan p;
+    int st = bragg_plan(d, &p);
+    if (st) return st;
+    if (mode != 0 && mode != 1) {
+        set_error("mode is 0 (march) or 1 (preconditioner)");
+        return DYFOX_EINVAL;
+    }
+    if (!y_values || !s_dev || !out || (mode == 1 && !in0) ||
+        (d->n_seg > 0 && !seg_table)) {
+        set_error("NULL argument to dyfox_bragg_apply");
+        return DYFOX_EINVAL;
+    }
+    if (workspace_bytes < p.ws || !workspace) {
+        set_error("workspace of %zu bytes, %zu needed", workspace_bytes, p.ws);
+        return DYFOX_ENOMEM;
+    }
+    const size_t smem = (size_t)3 * d->Nx * sizeof(double2) + 64;
+    if ((st = smem_ok(smem))) return st;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    BraggArgs a;
+    if ((st = bragg_prepare(d, p, seg_table, y_values, s_dev,
+                            (char *)workspace, stream, &a)))
+        return st;
+    const int nsys = d->n_y * d->n_s;
+    cudaError_t e;
+    const double2 *i0 = (const double2 *)in0, *i1 = (const double2 *)in1;
+    double2 *o = (double2 *)out;
+    switch (p.cpl) {
+    case 1: e = launch_apply<1>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
+    case 2: e = launch_apply<2>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
+    case 4: e = launch_apply<4>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
+    case 8: e = launch_apply<8>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
+    default: e = launch_apply<16>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
+    }
+    return cuda_status(e, "bragg_apply");
+}
+
+extern "C" int dyfox_bragg_symbol(const dyfox_bragg_desc *d,
+                                  const double *s_dev, void *T21, void *T22,
+                                  void *stream_) {
+    set_error("");
+    int st = bragg_validate(d);
+    if (st) return st;
+    if (!s_dev || (!T21 && !T22)) {
+        set_error("NULL argument to dyfox_bragg_symbol");
+        return DYFOX_EINVAL;
+    }
+    bragg_symbol_kernel<<<d->n_s, 256, 0, (cudaStream_t)stream_>>>(
+        s_dev, d->Nx, d->Nz, d->ds, d->sig0[0], d->sig0[1], d->sig_h[0],
+        d->sig_h[1], d->sig_hbar[0], d->sig_hbar[1], (double2 *)T21,
+        (double2 *)T22, nullptr);
+    count_launch(1);
+    return cuda_status(cudaGetLastError(), "bragg_symbol");
+}

@@ -1,0 +1,241 @@
+// Building blocks of the Bragg (reflection) shooting solve, one CTA per
+// system (y-plane x deviation parameter), everything in double:
+//   * complex helpers and CTA-wide reductions (warp shuffles + one shared
+//     slot per warp, fixed order, so results are deterministic);
+//   * the down-march of DYFOX bragg/solver.py:28-35 (the GMRES matvec);
+//   * a mixed-radix Stockham FFT in shared memory for the perfect-crystal
+//     preconditioner ifft(fft(w) / T22s) of bragg/solver.py:167-168.
+#pragma once
+#include "common.cuh"
+
+namespace dyfox {
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) {
+    return make_double2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ double2 csub(double2 a, double2 b) {
+    return make_double2(a.x - b.x, a.y - b.y);
+}
+__device__ __forceinline__ double2 cmulz(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// conj(a) * b
+__device__ __forceinline__ double2 cdotz(double2 a, double2 b) {
+    return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double2 cscale(double s, double2 a) {
+    return make_double2(s * a.x, s * a.y);
+}
+__device__ __forceinline__ double2 cconj(double2 a) {
+    return make_double2(a.x, -a.y);
+}
+__device__ __forceinline__ double cabs2(double2 a) {
+    return a.x * a.x + a.y * a.y;
+}
+
+// Sum of v over the CTA.  red: shared scratch of >= 33 double2.  Every
+// thread returns the total.  Two barriers.
+__device__ __forceinline__ double2 block_sum(double2 v, double2 *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double2 t = lane < nw ? red[lane] : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            t.x += __shfl_down_sync(0xffffffffu, t.x, o);
+            t.y += __shfl_down_sync(0xffffffffu, t.y, o);
+        }
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// Maximum over the CTA of a non-negative double.
+__device__ __forceinline__ double block_max(double v, double2 *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) red[warp].x = v;
+    __syncthreads();
+    if (warp == 0) {
+        double t = lane < nw ? red[lane].x : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            t = fmax(t, __shfl_down_sync(0xffffffffu, t, o));
+        if (lane == 0) red[32].x = t;
+    }
+    __syncthreads();
+    return red[32].x;
+}
+
+// ---------------------------------------------------------------------------
+// Down-march (bragg/solver.py:28-35): for k = 0 .. Nz-2
+//   D0'[x] = e0 (D0[x-1] + ds Cb[k][x-1] Dg[x-1])      (roll +1, periodic)
+//   Dg'[x] = (Dg[x+1] - ds Ch[k][x+1] D0[x+1]) / eg     (roll -1, periodic)
+// cb, ch: this plane's (Nz, Nx) couplings with ds folded in.  Column x is
+// held by thread x % nt in register slot x / nt; the shifted values pass
+// through the two shared exchange rows.  d0_in / dg_in NULL means zero.
+// Dg(t) is written to out (shared or global).
+template <int CPL>
+__device__ void bragg_march(const double2 *__restrict__ cb,
+                            const double2 *__restrict__ ch, double2 e0,
+                            double2 ieg, int Nz, int Nx,
+                            const double2 *d0_in, const double2 *dg_in,
+                            double2 *ex0, double2 *ex1, double2 *out) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    double2 D0[CPL], Dg[CPL];
+#pragma unroll
+    for (int i = 0; i < CPL; ++i) {
+        const int x = tid + i * nt;
+        D0[i] = make_double2(0.0, 0.0);
+        Dg[i] = make_double2(0.0, 0.0);
+        if (x < Nx) {
+            if (d0_in) D0[i] = d0_in[x];
+            if (dg_in) Dg[i] = dg_in[x];
+        }
+    }
+    for (int k = 0; k < Nz - 1; ++k) {
+        const double2 *cbk = cb + (size_t)k * Nx, *chk = ch + (size_t)k * Nx;
+#pragma unroll
+        for (int i = 0; i < CPL; ++i) {
+            const int x = tid + i * nt;
+            if (x < Nx) {
+                const double2 b = __ldg(cbk + x), h = __ldg(chk + x);
+                const double2 u = cadd(D0[i], cmulz(b, Dg[i]));
+                const double2 v = cmulz(csub(Dg[i], cmulz(h, D0[i])), ieg);
+                ex0[x + 1 == Nx ? 0 : x + 1] = cmulz(e0, u);
+                ex1[x == 0 ? Nx - 1 : x - 1] = v;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < CPL; ++i) {
+            const int x = tid + i * nt;
+            if (x < Nx) {
+                D0[i] = ex0[x];
+                Dg[i] = ex1[x];
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < CPL; ++i) {
+        const int x = tid + i * nt;
+        if (x < Nx) out[x] = Dg[i];
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-radix Stockham FFT (Govindaraju et al., SC'08 formulation): stage of
+// radix R over butterflies j in [0, N/R), Ns = product of earlier radices;
+// input index j + r N/R, output index (j / Ns) Ns R + j % Ns + q Ns.  The
+// twiddle exp(-+2 pi i r (j % Ns) / (Ns R)) and the radix-R DFT kernel both
+// come from the table tw[m] = exp(-2 pi i m / N).  Radix 2 and 4 use
+// explicit butterflies; other radices evaluate each output as an R-term sum
+// (N R complex products per stage).  inverse: conjugate twiddles, no scale.
+struct FftPlan {
+    int n;
+    int nfac;
+    int fac[24];
+};
+
+__device__ __forceinline__ double2 twid(const double2 *tw, int m, bool inv) {
+    double2 w = __ldg(tw + m);
+    return inv ? cconj(w) : w;
+}
+
+// Returns the buffer holding the result (src or dst).  All threads call.
+__device__ double2 *fft_run(double2 *src, double2 *dst, const FftPlan &p,
+                            const double2 *__restrict__ tw, bool inv) {
+    const int N = p.n, tid = threadIdx.x, nt = blockDim.x;
+    int Ns = 1;
+    for (int f = 0; f < p.nfac; ++f) {
+        const int R = p.fac[f];
+        const int nb = N / R;
+        const int step = N / (Ns * R);
+        if (R == 2) {
+            for (int j = tid; j < nb; j += nt) {
+                const int k = j % Ns;
+                double2 a = src[j], b = src[j + nb];
+                if (k) b = cmulz(b, twid(tw, k * step, inv));
+                const int d = (j / Ns) * Ns * 2 + k;
+                dst[d] = cadd(a, b);
+                dst[d + Ns] = csub(a, b);
+            }
+        } else if (R == 4) {
+            for (int j = tid; j < nb; j += nt) {
+                const int k = j % Ns;
+                double2 v0 = src[j], v1 = src[j + nb], v2 = src[j + 2 * nb],
+                        v3 = src[j + 3 * nb];
+                if (k) {
+                    v1 = cmulz(v1, twid(tw, k * step, inv));
+                    v2 = cmulz(v2, twid(tw, 2 * k * step, inv));
+                    v3 = cmulz(v3, twid(tw, 3 * k * step, inv));
+                }
+                const double2 s02 = cadd(v0, v2), d02 = csub(v0, v2);
+                const double2 s13 = cadd(v1, v3), d13 = csub(v1, v3);
+                // -i d13 forward, +i d13 inverse
+                const double2 rot = inv ? make_double2(-d13.y, d13.x)
+                                        : make_double2(d13.y, -d13.x);
+                const int d = (j / Ns) * Ns * 4 + k;
+                dst[d] = cadd(s02, s13);
+                dst[d + Ns] = cadd(d02, rot);
+                dst[d + 2 * Ns] = csub(s02, s13);
+                dst[d + 3 * Ns] = csub(d02, rot);
+            }
+        } else {
+            for (int it = tid; it < N; it += nt) {
+                const int j = it % nb, q = it / nb;
+                const int k = j % Ns;
+                // sum_r src[j + r nb] W^(r (k step + q nb))
+                int base = k * step + q * nb;
+                if (base >= N) base -= N;
+                double2 acc = src[j];
+                int m = base;
+                for (int r = 1; r < R; ++r) {
+                    acc = cadd(acc, cmulz(src[j + r * nb], twid(tw, m, inv)));
+                    m += base;
+                    if (m >= N) m -= N;
+                }
+                dst[(j / Ns) * Ns * R + k + q * Ns] = acc;
+            }
+        }
+        __syncthreads();
+        double2 *t = src;
+        src = dst;
+        dst = t;
+        Ns *= R;
+    }
+    return src;
+}
+
+// w <- ifft(fft(w) * iT) with iT = 1 / T22s; a, b are scratch rows.
+__device__ void precond_apply(double2 *w, double2 *a, double2 *b,
+                              const FftPlan &p,
+                              const double2 *__restrict__ tw,
+                              const double2 *__restrict__ iT) {
+    const int N = p.n, tid = threadIdx.x, nt = blockDim.x;
+    for (int x = tid; x < N; x += nt) a[x] = w[x];
+    __syncthreads();
+    double2 *f = fft_run(a, b, p, tw, false);
+    for (int x = tid; x < N; x += nt) f[x] = cmulz(f[x], __ldg(iT + x));
+    __syncthreads();
+    double2 *o = f == a ? b : a;
+    double2 *g = fft_run(f, o, p, tw, true);
+    const double inv_n = 1.0 / N;
+    for (int x = tid; x < N; x += nt) w[x] = cscale(inv_n, g[x]);
+    __syncthreads();
+}
+
+}  // namespace dyfox

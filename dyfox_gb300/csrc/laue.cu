@@ -178,17 +178,22 @@ __global__ void laue_general_kernel(const MarchArgs a, R shift_px) {
 #undef ST
 }
 
-// Rows with |y| >= fov_hy are written as zero (kernels.py:70-75).
+// Rows with |y| >= fov_hy are written as zero (kernels.py:70-75).  Rows
+// start on 8-byte boundaries (complex64 or complex128 elements), so the
+// stores are 8 bytes wide; blocks stride over the (angle, row) pairs.
 __global__ void zero_rows_kernel(char *out, int n_e, int Ny, size_t row_bytes,
                                  int row0, int n_rows) {
     const int n_inactive = Ny - n_rows;
-    const long r = blockIdx.y;                 // (angle, inactive row)
-    const int ie = (int)(r / n_inactive), j = (int)(r - (long)ie * n_inactive);
-    const int iy = j < row0 ? j : j + n_rows;
-    uint4 *p = reinterpret_cast<uint4 *>(out + ((size_t)ie * Ny + iy) * row_bytes);
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-         i < row_bytes / 16; i += (size_t)gridDim.x * blockDim.x)
-        p[i] = make_uint4(0, 0, 0, 0);
+    const long pairs = (long)n_e * n_inactive;
+    const size_t words = row_bytes / 8;
+    for (long r = blockIdx.x; r < pairs; r += gridDim.x) {
+        const int ie = (int)(r / n_inactive);
+        const int j = (int)(r - (long)ie * n_inactive);
+        const int iy = j < row0 ? j : j + n_rows;
+        uint2 *p = reinterpret_cast<uint2 *>(out + ((size_t)ie * Ny + iy) * row_bytes);
+        for (size_t i = threadIdx.x; i < words; i += blockDim.x)
+            p[i] = make_uint2(0, 0);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -430,10 +435,9 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     cudaError_t e;
     // Rows outside the beam are zero.
     if (p.n_rows < d->Ny) {
-        size_t row_bytes = (size_t)d->Nx * elem;
-        dim3 grid(div_up((int)(row_bytes / 16), 256) < 64
-                      ? div_up((int)(row_bytes / 16), 256) : 64,
-                  d->n_e * (d->Ny - p.n_rows));
+        const size_t row_bytes = (size_t)d->Nx * elem;
+        const long pairs = (long)d->n_e * (d->Ny - p.n_rows);
+        const int grid = pairs < 152L * 16 ? (int)pairs : 152 * 16;
         zero_rows_kernel<<<grid, 256, 0, stream>>>((char *)out, d->n_e, d->Ny,
                                                    row_bytes, p.row0, p.n_rows);
         count_launch(1);

@@ -124,6 +124,60 @@ int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
                      const void *h_grid, const double *seg_table, void *out,
                      void *workspace, size_t workspace_bytes, void *stream);
 
+typedef struct dyfox_bragg_desc {
+    double sig0[2], sig_h[2], sig_hbar[2];   /* (re, im), 1/m              */
+    int Nx, Nz;                              /* BraggConfig.Nx, .Nz        */
+    double dx, dz, ds;                       /* BraggConfig.dx, .dz, .ds   */
+    int n_y;                                 /* y-planes per deviation     */
+    int n_s;                                 /* deviation parameters       */
+    int n_seg;                               /* segment table entries      */
+    double nu, a_core;
+    int beam;                                /* 0 plane wave, 1 top hat    */
+    double beam_thickness, beam_centre;      /* top hat (BraggConfig)      */
+    double tol;                              /* GMRES rtol (true residual) */
+    int restart, maxiter;                    /* GMRES restart, maxiter     */
+    int precision;                           /* DYFOX_FP64                 */
+    unsigned flags;                          /* reserved, 0                */
+} dyfox_bragg_desc;
+
+/* Workspace bytes of dyfox_bragg_solve / dyfox_bragg_apply. */
+size_t dyfox_bragg_workspace_bytes(const dyfox_bragg_desc *d);
+
+/* Surface exit waves of n_s x n_y independent shooting problems (every
+ * deviation parameter on every y-plane), each solved by its own
+ * left-preconditioned restarted GMRES to true relative residual <= tol.
+ * Replaces solve_surface_batch and solve_bragg_stable (bragg/solver.py:
+ * 135-379) including the Volterra phase of each plane (H_plane, dislocations
+ * .py:171-211), the couplings (solver.py:256-261), the particular march
+ * (263-265), the perfect-crystal preconditioner (270-278) and the phase
+ * restoration v e^{-iH(0)} (362-373).
+ * seg_table: device; y_values: HOST, n_y doubles; s_dev: device, n_s;
+ * x0: device (n_s, n_y, Nx) complex128 warm start, or NULL for zero;
+ * out: device (n_s, n_y, Nx) complex128; info: device (n_s * n_y, 4)
+ * doubles per system: true relative residual, inner iterations, code (0
+ * converged, else maxiter), |b|; or NULL. */
+int dyfox_bragg_solve(const dyfox_bragg_desc *d, const double *seg_table,
+                      const double *y_values, const double *s_dev,
+                      const void *x0, void *out, double *info,
+                      void *workspace, size_t workspace_bytes, void *stream);
+
+/* One operator application per system, for parity checks.
+ * mode 0: out = down-march of (D0(0), Dg(0)) = (in0, in1) to D_g(t)
+ *         (bragg/solver.py:28-35; NULL input = zero);
+ * mode 1: out = ifft(fft(in0) / T22s) (solver.py:167-168, 297-300).
+ * in0, in1, out: device (n_s, n_y, Nx) complex128. */
+int dyfox_bragg_apply(const dyfox_bragg_desc *d, int mode,
+                      const double *seg_table, const double *y_values,
+                      const double *s_dev, const void *in0, const void *in1,
+                      void *out, void *workspace, size_t workspace_bytes,
+                      void *stream);
+
+/* Fourier symbol of the perfect-crystal shooting operator per deviation
+ * parameter: T21, T22 (device, (n_s, Nx) complex128; either may be NULL).
+ * Replaces bragg.perfect_symbol (bragg/solver.py:38-60). */
+int dyfox_bragg_symbol(const dyfox_bragg_desc *d, const double *s_dev,
+                       void *T21, void *T22, void *stream);
+
 /* Diagnostic (not part of any DYFOX interface): measured FMA throughput
  * of this GPU in TFLOP/s (2 flops per FMA) for DYFOX_FP64 or DYFOX_FP32,
  * the denominator of the arithmetic-bound kernels' roofline.  Synchronises

@@ -1,0 +1,182 @@
+"""The CUDA Bragg shooting solve against the reference's golden vectors and
+the NumPy oracle.
+
+Tolerances: the march (the GMRES matvec), the perfect-crystal symbol and
+the preconditioner match to <= 1e-12 relative L2; solutions, which carry the
+GMRES tolerance (1e-10 true relative residual), match the oracle's dense
+direct solve to <= 1e-8 and the reference's GMRES answers to <= 1e-7 (the
+reference's own batched-vs-single tolerance, tests/test_bragg.py:155-167).
+"""
+
+import numpy as np
+import pytest
+
+from conftest import golden, rel_l2
+from oracle import bragg_oracle as BO
+from oracle import closed_forms as CF
+
+pytestmark = pytest.mark.gpu
+
+OP_TOL = 1e-12
+
+
+def np_(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def small(diamond400):
+    from dyfox_gb300.bragg_geometry import BraggConfig, bragg_g_vector
+    b = golden("bragg_small")
+    t, dx, hx = b["cfg"][:3]
+    cfg = BraggConfig(diamond400, t_crystal=t, dx=dx, half_x=hx)
+    seg = [(q[:3], q[3:6], q[6:]) for q in b["segs"]]
+    return b, cfg, seg, bragg_g_vector(diamond400)
+
+
+def test_march_matches_the_reference(gpu, diamond400, small):
+    from dyfox_gb300.bragg import apply_operator
+    torch = gpu
+    b, cfg, seg, g = small
+    s = [float(b["s_dev"])]
+    inc = torch.ones((1, 1, cfg.Nx), dtype=torch.complex128, device="cuda")
+    d = np_(apply_operator(seg, s, cfg, [0.0], diamond400, g, "march",
+                           in0=inc))[0, 0]
+    assert rel_l2(d, b["d"]) < OP_TOL
+    v = torch.from_numpy(b["v"]).to("cuda").reshape(1, 1, -1)
+    Av = np_(apply_operator(seg, s, cfg, [0.0], diamond400, g, "march",
+                            in1=v))[0, 0]
+    assert rel_l2(Av, b["Av"]) < OP_TOL
+
+
+def test_march_matches_the_oracle_on_many_planes(gpu, diamond400, small,
+                                                 rng):
+    from dyfox_gb300.bragg import apply_operator
+    torch = gpu
+    b, cfg, seg, g = small
+    s = [float(b["s_dev"]), 3e5]
+    ys = np.array([-0.3e-6, 0.05e-6, 0.6e-6])
+    v = rng.normal(size=(2, 3, cfg.Nx)) + 1j * rng.normal(size=(2, 3, cfg.Nx))
+    got = np_(apply_operator(seg, s, cfg, ys, diamond400, g, "march",
+                             in1=torch.from_numpy(v).to("cuda")))
+    for i, sv in enumerate(s):
+        for j, y in enumerate(ys):
+            mv, _, _, _ = BO.system(seg, sv, cfg, diamond400, g, y)
+            assert rel_l2(got[i, j], mv(v[i, j])) < OP_TOL
+
+
+def test_perfect_symbol_matches_the_reference(gpu, diamond400, small):
+    from dyfox_gb300.bragg import perfect_symbol
+    b, cfg, seg, g = small
+    e0, eg = BO.step_factors(diamond400, float(b["s_dev"]), cfg.ds)
+    T21, T22 = perfect_symbol(e0, eg, cfg.ds, cfg.Nz, cfg.Nx, diamond400)
+    assert rel_l2(T21, b["T21"]) < OP_TOL
+    assert rel_l2(T22, b["T22"]) < OP_TOL
+
+
+@pytest.mark.parametrize("nx_case", ["small", "cfg1"])
+def test_preconditioner_matches_numpy(gpu, diamond400, small, rng, nx_case):
+    """ifft(fft(w) / T22s) with the mixed-radix FFT (632 = 4 2 79 and
+    456 = 4 2 3 19)."""
+    from dyfox_gb300.bragg import apply_operator
+    from dyfox_gb300.bragg_geometry import BraggConfig
+    torch = gpu
+    b, cfg, seg, g = small
+    if nx_case == "cfg1":
+        cfg = BraggConfig(diamond400, t_crystal=20e-6, dx=0.5e-6,
+                          half_x=16e-6)
+        assert cfg.Nx == 456
+    s = [float(b["s_dev"]), -2e5]
+    w = rng.normal(size=(2, 1, cfg.Nx)) + 1j * rng.normal(size=(2, 1, cfg.Nx))
+    got = np_(apply_operator(seg, s, cfg, [0.0], diamond400, g, "precond",
+                             in0=torch.from_numpy(w).to("cuda")))
+    for i, sv in enumerate(s):
+        e0, eg = BO.step_factors(diamond400, sv, cfg.ds)
+        _, T22 = BO.perfect_symbol(e0, eg, cfg.ds, cfg.Nz, cfg.Nx, diamond400)
+        want = BO.precondition(w[i, 0], BO.floored(T22))
+        assert rel_l2(got[i, 0], want) < OP_TOL
+
+
+def test_single_plane_solve(gpu, diamond400, small):
+    from dyfox_gb300.bragg import solve_bragg_stable
+    b, cfg, seg, g = small
+    s = float(b["s_dev"])
+    wave, info = solve_bragg_stable(seg, s, cfg, diamond400, g)
+    assert info["gmres_code"] == 0 and info["residual"] < 1e-10
+    assert set(info) == {"gmres_code", "iterations", "residual"}
+    dense, _ = BO.dense_solve(seg, s, cfg, diamond400, g)
+    assert rel_l2(wave, dense) < 1e-8
+    assert rel_l2(wave, b["exit_wave"]) < 1e-7
+
+
+def test_surface_batch_matches_the_reference(gpu, diamond400, small):
+    from dyfox_gb300.bragg import solve_surface_batch
+    b, cfg, seg, g = small
+    out, info = solve_surface_batch(seg, float(b["s_dev"]), cfg, b["ys"],
+                                    diamond400, g)
+    assert isinstance(out, np.ndarray) and out.dtype == np.complex128
+    assert info["converged"] and info["residual"] < 1e-7
+    for key in ("residual", "iterations", "retries", "splits",
+                "unconverged_chunks", "converged"):
+        assert key in info
+    for j in range(len(b["ys"])):
+        assert np.abs(out[j] - b["surface"][j]).max() < \
+            1e-7 * np.abs(b["surface"][j]).max()
+
+
+def test_batched_scan_equals_single_calls(gpu, diamond400, small):
+    from dyfox_gb300.bragg import solve_scan, solve_surface_batch
+    b, cfg, seg, g = small
+    s = [float(b["s_dev"]), -1e5, 2e5]
+    ys = b["ys"]
+    out, info = solve_scan(seg, s, cfg, ys, diamond400, g)
+    out = np_(out)
+    for i, sv in enumerate(s):
+        one, _ = solve_surface_batch(seg, sv, cfg, ys, diamond400, g)
+        assert np.array_equal(out[i], one)
+    assert float(info[:, 0].max()) < 1e-10
+
+
+def test_chunk_size_changes_nothing(gpu, diamond400, small):
+    from dyfox_gb300.bragg import solve_surface_batch
+    b, cfg, seg, g = small
+    ys = (np.arange(6) - 3) * cfg.dx
+    a, ia = solve_surface_batch(seg, float(b["s_dev"]), cfg, ys, diamond400,
+                                g, chunk=16)
+    c, ic = solve_surface_batch(seg, float(b["s_dev"]), cfg, ys, diamond400,
+                                g, chunk=1)
+    assert ia["converged"] and ic["converged"]
+    assert np.array_equal(a, c)
+
+
+def test_zero_burgers_vector_is_a_perfect_crystal(gpu, diamond400, small):
+    from dyfox_gb300.bragg import solve_bragg_stable
+    b, cfg, seg, g = small
+    dead = [(seg[0][0], seg[0][1], np.zeros(3))]
+    s = float(b["s_dev"])
+    with_zero, _ = solve_bragg_stable(dead, s, cfg, diamond400, g)
+    pristine, _ = solve_bragg_stable([], s, cfg, diamond400, g)
+    assert np.abs(with_zero - pristine).max() < 1e-12
+    assert rel_l2(pristine, b["exit_wave_pristine"]) < 1e-7
+
+
+def test_pristine_reflectivity_matches_riccati(gpu, diamond400, small):
+    """The perfect crystal on the grid against the finite-thickness Riccati
+    closed form: agreement to the discretisation error of the grid."""
+    from dyfox_gb300.bragg import solve_surface_batch
+    from dyfox_gb300.units import deviation_from_urad
+    b, cfg, seg, g = small
+    for urad, want in zip(b["riccati_urad"], b["riccati_6um"]):
+        sd = float(deviation_from_urad(urad, diamond400))
+        out, info = solve_surface_batch([], sd, cfg, [0.0], diamond400, g)
+        assert info["converged"]
+        mine = abs(out[0, cfg.Nx // 2])
+        assert mine == pytest.approx(abs(want), rel=3e-3)
+        assert np.abs(out).max() <= 1.0 + 1e-9
+
+
+def test_bad_deviation_is_rejected(gpu, diamond400, small):
+    from dyfox_gb300.bragg import solve_surface_batch
+    b, cfg, seg, g = small
+    with pytest.raises(ValueError):
+        solve_surface_batch(seg, float("nan"), cfg, [0.0], diamond400, g)

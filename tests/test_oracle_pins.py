@@ -158,3 +158,40 @@ def test_closed_forms_match_the_reference(diamond400):
     Nz, dz = b["cfg"][3], b["cfg"][5]
     got = CF.reflectivity_riccati(sd, float((Nz - 1) * dz), diamond400)
     np.testing.assert_allclose(got, b["riccati_6um"], rtol=1e-9)
+
+
+# ------------------------------------------------------------------- Bragg
+def _bragg_small(diamond400):
+    from dyfox_gb300.bragg_geometry import BraggConfig, bragg_g_vector
+    b = golden("bragg_small")
+    t, dx, hx = b["cfg"][:3]
+    cfg = BraggConfig(diamond400, t_crystal=t, dx=dx, half_x=hx)
+    seg = [(q[:3], q[3:6], q[6:]) for q in b["segs"]]
+    return b, cfg, seg, bragg_g_vector(diamond400)
+
+
+def test_bragg_oracle_march_and_symbol_match_the_reference(diamond400):
+    from oracle import bragg_oracle as BO
+    b, cfg, seg, g = _bragg_small(diamond400)
+    s = float(b["s_dev"])
+    matvec, d, H, T22s = BO.system(seg, s, cfg, diamond400, g)
+    np.testing.assert_allclose(H[0], b["H_row0"], rtol=0, atol=1e-13)
+    assert rel_l2(d, b["d"]) < 1e-12
+    assert rel_l2(matvec(b["v"]), b["Av"]) < 1e-12
+    e0, eg = BO.step_factors(diamond400, s, cfg.ds)
+    T21, T22 = BO.perfect_symbol(e0, eg, cfg.ds, cfg.Nz, cfg.Nx, diamond400)
+    assert rel_l2(T21, b["T21"]) < 1e-14 and rel_l2(T22, b["T22"]) < 1e-14
+
+
+def test_bragg_oracle_solutions_match_the_reference(diamond400):
+    from oracle import bragg_oracle as BO
+    b, cfg, seg, g = _bragg_small(diamond400)
+    s = float(b["s_dev"])
+    ew, v, res, code = BO.solve_plane(seg, s, cfg, diamond400, g)
+    assert code == 0 and res < 1e-10
+    assert rel_l2(ew, b["exit_wave"]) < 1e-8
+    dense, _ = BO.dense_solve(seg, s, cfg, diamond400, g)
+    assert rel_l2(dense, b["exit_wave"]) < 1e-8
+    out, info = BO.solve_surface(seg, s, cfg, b["ys"], diamond400, g)
+    assert info["converged"]
+    assert rel_l2(out, b["surface"]) < 1e-8
