@@ -17,6 +17,7 @@ DYFOX_EMAXITER, DYFOX_ENAN, DYFOX_ECUDA, DYFOX_ENOSYS = 4, 5, 6, 7
 DYFOX_FP64, DYFOX_FP32 = 0, 1
 H_NONE, H_GRID_F64, H_GRID_F32, H_SEGMENTS, H_ANALYTIC = 0, 1, 2, 3, 4
 FLAG_FUSED, FLAG_STAGED, FLAG_NO_COMP, FLAG_GENERAL = 1, 2, 4, 8
+FLAG_H_FP64 = 16
 SEG_STRIDE = 24
 
 

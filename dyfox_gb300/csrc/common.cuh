@@ -28,7 +28,7 @@ enum SegField {
     SEG_KL = 17,                         // coefficient of ln r2c
     SEG_KQ = 18,                         // coefficient of (d1^2-d2^2)/r2c
     SEG_HCONST = 19,                     // K_l ln(dx^2), kept in double
-    SEG_DX = 20,                         // pixel pitch of the scaling
+    SEG_C1 = 20,                         // b_perp / (2 pi)
     SEG_A2PX = 21,                       // (a_core / dx)^2
     SEG_SLOPE1 = 22, SEG_SLOPE2 = 23     // d(d1)/dx, d(d2)/dx along a row
 };

@@ -10,8 +10,8 @@
 namespace dyfox {
 
 // cs staging, defined in volterra.cu.
-cudaError_t launch_cs_stage(bool single, const double *segs, int n_seg,
-                            int Nx, int Ny, int Nz, double dx,
+cudaError_t launch_cs_stage(bool single, bool sum64, const double *segs,
+                            int n_seg, int Nx, int Ny, int Nz, double dx,
                             double dz, const VolterraConsts &vc, int row0,
                             int n_rows, void *out, cudaStream_t stream);
 
@@ -202,7 +202,7 @@ struct LauePlan {
     int hsrc = HS_NONE;      // source the march kernel reads
     int stage = 0;           // 0: none, 1: stage e^{iH} (CS32/CS64)
     int row0 = 0, n_rows = 0;
-    size_t off_kappa = 0, off_scale = 0, off_stage = 0, ws = 0;
+    size_t off_kappa = 0, off_scale = 0, off_stage = 0, off_piv = 0, ws = 0;
 };
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -286,6 +286,10 @@ static int make_plan(const dyfox_laue_desc *d, LauePlan *p) {
     if (p->stage)
         off = align256(off + (size_t)p->n_rows * (d->Nz - 1) * d->Nx *
                                  (single ? sizeof(float2) : sizeof(double2)));
+    p->off_piv = off;
+    if (p->hsrc == HS_SEG && single)
+        off = align256(off + (size_t)p->n_rows * (d->Nz - 1) * d->n_seg *
+                                 sizeof(float4));
     p->ws = off;
     return DYFOX_OK;
 }
@@ -300,7 +304,9 @@ static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
                        FastConfig *fc) {
     const bool single = d->precision == DYFOX_FP32;
     const bool comp = single && !(d->flags & DYFOX_FLAG_NO_COMP);
-    const int ht = p.hsrc == HS_SEG ? HT_SEG : HT_GENERIC;
+    const int ht = p.hsrc != HS_SEG ? HT_GENERIC
+                   : (single && (d->flags & DYFOX_FLAG_H_FP64)) ? HT_SEG64
+                                                                : HT_SEG;
     const int *cpls = single ? kCplF32 : kCplF64;
     const int ncpl = single ? kNumCplF32 : kNumCplF64;
     // Columns per lane: the fewest padded columns; ties go to more columns
@@ -431,6 +437,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     a.scale = (const double2 *)(ws + p.off_scale);
     a.out = out;
     a.csgrid = ws + p.off_stage;
+    a.piv = (const float4 *)(ws + p.off_piv);
 
     cudaError_t e;
     // Rows outside the beam are zero.
@@ -454,8 +461,19 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
         count_launch(1);
         if ((e = cudaGetLastError())) return cuda_status(e, "laue_setup");
     }
+    if (p.hsrc == HS_SEG && single) {
+        const long n = (long)p.n_rows * nsteps * d->n_seg;
+        long blocks = (n + 255) / 256;
+        if (blocks > 152L * 32) blocks = 152L * 32;
+        pivot_kernel<<<(int)blocks, 256, 0, stream>>>(
+            seg_table, d->n_seg, d->Nx, d->Ny, d->dx, d->dz, p.row0, p.n_rows,
+            nsteps, (float4 *)(ws + p.off_piv));
+        count_launch(1);
+        if ((e = cudaGetLastError())) return cuda_status(e, "pivot");
+    }
     if (p.stage) {
-        e = launch_cs_stage(single, seg_table, d->n_seg, d->Nx, d->Ny,
+        e = launch_cs_stage(single, (d->flags & DYFOX_FLAG_H_FP64) != 0,
+                            seg_table, d->n_seg, d->Nx, d->Ny,
                             d->Nz, d->dx, d->dz, a.vc, p.row0, p.n_rows,
                             ws + p.off_stage, stream);
         if (e) return cuda_status(e, "cs_stage");

@@ -4,17 +4,17 @@
 namespace dyfox {
 
 #define DYFOX_E32(CPL, HT)                                                   \
-    case (CPL) * 2 + (HT):                                                   \
+    case (CPL) * 4 + (HT):                                                   \
         return {launch_march<float, CPL, HT, false>,                          \
                 attr_march<float, CPL, HT, false>};
 
 MarchEntry march_entry_f32_plain(int cpl, int ht) {
-    switch (cpl * 2 + ht) {
-        DYFOX_E32(5, 0) DYFOX_E32(5, 1)
-        DYFOX_E32(7, 0) DYFOX_E32(7, 1)
-        DYFOX_E32(9, 0) DYFOX_E32(9, 1)
-        DYFOX_E32(11, 0) DYFOX_E32(11, 1)
-        DYFOX_E32(13, 0) DYFOX_E32(13, 1)
+    switch (cpl * 4 + ht) {
+        DYFOX_E32(5, 0) DYFOX_E32(5, 1) DYFOX_E32(5, 2)
+        DYFOX_E32(7, 0) DYFOX_E32(7, 1) DYFOX_E32(7, 2)
+        DYFOX_E32(9, 0) DYFOX_E32(9, 1) DYFOX_E32(9, 2)
+        DYFOX_E32(11, 0) DYFOX_E32(11, 1) DYFOX_E32(11, 2)
+        DYFOX_E32(13, 0) DYFOX_E32(13, 1) DYFOX_E32(13, 2)
     default:
         return {nullptr, nullptr};
     }

@@ -32,7 +32,12 @@ namespace dyfox {
 
 enum HSrc { HS_NONE = 0, HS_GRID64 = 1, HS_GRID32 = 2, HS_CS32 = 3,
             HS_SEG = 4, HS_ANALYTIC = 5, HS_CS64 = 6 };
-enum HTemplate { HT_GENERIC = 0, HT_SEG = 1 };
+// H source compiled into a march: cheap sources chosen at run time, or the
+// Volterra field of the segments evaluated per voxel.  In single precision
+// HT_SEG sums the segment terms in float-float (two-sum) and reduces mod
+// 2 pi in single precision; HT_SEG64 sums and reduces in double.  In double
+// precision HT_SEG is the reference-order double evaluation.
+enum HTemplate { HT_GENERIC = 0, HT_SEG = 1, HT_SEG64 = 2 };
 
 // Interaction-picture coupling constants of one (angle, step).
 struct Kappa {
@@ -56,6 +61,7 @@ struct MarchArgs {
     const void *csgrid;         // CS32 / CS64: staged e^{iH} as float2 /
                                 // double2, (n_rows, Nz - 1, Nx), row-relative
     const double *segs;         // SEG: segment table
+    const float4 *piv;          // SEG single: pivots (n_rows, Nz - 1, n_seg)
     int n_seg;
     VolterraConsts vc;
     double an[12];              // ANALYTIC
@@ -167,8 +173,6 @@ __host__ __device__ inline MarchSmem march_smem(int CPL, int WA, int A,
     if (hsrc == HS_SEG && sizeof(R) == 4) off += (size_t)n_seg * sizeof(SegF);
     off = (off + 15) & ~(size_t)15;
     m.piv = off;
-    if (hsrc == HS_SEG && sizeof(R) == 4)
-        off += (size_t)2 * n_seg * sizeof(float4);
     m.hc = off;
     off += sizeof(double);
     m.total = off;
@@ -192,38 +196,37 @@ __global__ void laue_march_kernel(const MarchArgs a) {
     const int ie_raw = grp * a.A + g;
     const int ie = ie_raw < a.n_e ? ie_raw : a.n_e - 1;
     const int Nx = a.Nx, Nz = a.Nz, nsteps = Nz - 1;
-    const int hsrc = HT == HT_SEG ? HS_SEG : a.hsrc;
+    const int hsrc = HT != HT_GENERIC ? HS_SEG : a.hsrc;
     const MarchSmem plan = march_smem<R>(CPL, WA, a.A, Nz, hsrc, a.n_seg,
                                          COMP);
     R2 *cs = reinterpret_cast<R2 *>(smem + plan.cs);
     R2 *bnd = reinterpret_cast<R2 *>(smem + plan.bnd);
     R2 *an_cs = reinterpret_cast<R2 *>(smem + plan.an);
     SegF *segf = reinterpret_cast<SegF *>(smem + plan.segf);
-    float4 *piv = reinterpret_cast<float4 *>(smem + plan.piv);
     double *hc_sm = reinterpret_cast<double *>(smem + plan.hc);
     const int NB = COMP ? 4 : 2;
     const double y_pix = (iy - a.Ny / 2) * a.dx;
     constexpr bool kSingle = sizeof(R) == 4;
 
     // ---------------------------------------------------------- prologue
-    if (HT == HT_SEG && kSingle) {
+    if (HT != HT_GENERIC && kSingle) {
         if (tid == 0) *hc_sm = sum_hconst(a.segs, a.n_seg);
-        for (int s = tid; s < a.n_seg; s += nthreads) {
-            const double *sg = a.segs + (size_t)s * DYFOX_SEG_STRIDE;
-            segf[s] = seg_f32(sg);
-            piv[s] = seg_pivot(sg, y_pix, 0.0, Nx, a.dx);
-            if (nsteps > 1)
-                piv[a.n_seg + s] = seg_pivot(sg, y_pix, a.dz, Nx, a.dx);
-        }
+        for (int s = tid; s < a.n_seg; s += nthreads)
+            segf[s] = seg_f32(a.segs + (size_t)s * DYFOX_SEG_STRIDE);
     }
     if (HT == HT_GENERIC && hsrc == HS_ANALYTIC) {
         for (int k = tid; k < nsteps; k += nthreads)
             an_cs[k] = CS<R>::of_f64(analytic_h(a.an, y_pix, k, a.dz));
     }
-    if ((HT == HT_SEG && kSingle) || hsrc == HS_ANALYTIC) __syncthreads();
-    // Sum over segments of the constant the single evaluator drops.
+    if ((HT != HT_GENERIC && kSingle) || hsrc == HS_ANALYTIC) __syncthreads();
+    // Sum over segments of the constant the single evaluator drops (double),
+    // and that sum reduced mod 2 pi (start of the float-float sum).
     double hconst = 0.0;
-    if (HT == HT_SEG && kSingle) hconst = *hc_sm;
+    float hcr = 0.0f;
+    if (HT != HT_GENERIC && kSingle) {
+        hconst = *hc_sm;
+        hcr = reduce_2pi(hconst);
+    }
 
     // Produces e^{iH(kk, x)} of every padded column into buffer `buf`.
     auto produce = [&](int kk, int buf) {
@@ -235,13 +238,28 @@ __global__ void laue_march_kernel(const MarchArgs a) {
             R2 v;
             if (x >= Nx) {
                 v.x = R(0); v.y = R(0);
-            } else if (HT == HT_SEG) {
-                if (kSingle) {
-                    const float4 *pv = piv + (size_t)(kk & 1) * a.n_seg;
-                    double acc = hconst;
-                    for (int s = 0; s < a.n_seg; ++s)
-                        acc += (double)h_seg_f32(segf[s], pv[s], x);
-                    v = CS<R>::of_f64(acc);
+            } else if (HT != HT_GENERIC) {
+                if constexpr (kSingle) {
+                    const float4 *pv =
+                        a.piv + ((size_t)row_blk * nsteps + kk) * a.n_seg;
+                    if constexpr (HT == HT_SEG) {
+                        float hi = hcr, lo = 0.0f;
+                        for (int s = 0; s < a.n_seg; ++s) {
+                            float e;
+                            hi = two_sum(hi, h_seg_f32(segf[s], __ldg(pv + s), x),
+                                         e);
+                            lo += e;
+                        }
+                        float sn, c;
+                        sincosf(reduce_2pi_ff(hi, lo), &sn, &c);
+                        v.x = c;
+                        v.y = sn;
+                    } else {
+                        double acc = hconst;
+                        for (int s = 0; s < a.n_seg; ++s)
+                            acc += (double)h_seg_f32(segf[s], __ldg(pv + s), x);
+                        v = CS<R>::of_f64(acc);
+                    }
                 } else {
                     const double X0 = __dmul_rn((double)x - 0.5 * Nx, a.dx);
                     const double yv = __dmul_rn((double)iy - 0.5 * a.Ny, a.dx);
@@ -318,12 +336,6 @@ __global__ void laue_march_kernel(const MarchArgs a) {
         const int p = k & 1;
         const Kappa kk4 = kn;
         if (k + 1 < nsteps) kn = ldg_kappa(kap + k + 1);
-        if (HT == HT_SEG && kSingle && k + 2 < nsteps) {
-            for (int s = tid; s < a.n_seg; s += nthreads)
-                piv[(size_t)(k & 1) * a.n_seg + s] = seg_pivot(
-                    a.segs + (size_t)s * DYFOX_SEG_STRIDE, y_pix,
-                    (k + 2) * a.dz, Nx, a.dx);
-        }
         if (k + 1 < nsteps) produce(k + 1, p ^ 1);
 
         const R k12r = (R)kk4.k12.x, k12i = (R)kk4.k12.y;

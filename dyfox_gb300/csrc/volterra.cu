@@ -67,7 +67,7 @@ static int launch_h_rows(bool f32out, const double *segs, int n_seg, int Nx,
 // terms in single, their sum and the 2 pi reduction in double.
 constexpr int kStageKB = 4;
 
-template <bool SINGLE>
+template <bool SINGLE, bool SUM64>
 __global__ void cs_stage_kernel(const double *__restrict__ segs, int n_seg,
                                 int Nx, int Ny, int Nz, double dx, double dz,
                                 VolterraConsts vc, int row0, int n_rows,
@@ -95,14 +95,28 @@ __global__ void cs_stage_kernel(const double *__restrict__ segs, int n_seg,
         }
         __syncthreads();
         const double hconst = *hc;
+        const float hcr = reduce_2pi(hconst);
         for (int j = tid; j < kn * Nx; j += nt) {
             const int kb = j / Nx, x = j - kb * Nx;
-            double acc = hconst;
             const float4 *pv = piv + (size_t)kb * n_seg;
-            for (int s = 0; s < n_seg; ++s)
-                acc += (double)h_seg_f32(segf[s], pv[s], x);
+            float r;
+            if (SUM64) {
+                double acc = hconst;
+                for (int s = 0; s < n_seg; ++s)
+                    acc += (double)h_seg_f32(segf[s], pv[s], x);
+                r = reduce_2pi(acc);
+            } else {
+                float hi = hcr, lo = 0.0f;
+                for (int s = 0; s < n_seg; ++s) {
+                    const float h = h_seg_f32(segf[s], pv[s], x);
+                    const float sum = hi + h, bb = sum - hi;
+                    lo += (hi - (sum - bb)) + (h - bb);
+                    hi = sum;
+                }
+                r = reduce_2pi_ff(hi, lo);
+            }
             float sn, c;
-            sincosf(reduce_2pi(acc), &sn, &c);
+            sincosf(r, &sn, &c);
             ((float2 *)out)[((size_t)r * nsteps + k0 + kb) * Nx + x] =
                 make_float2(c, sn);
         }
@@ -127,8 +141,25 @@ __global__ void cs_stage_kernel(const double *__restrict__ segs, int n_seg,
     }
 }
 
-cudaError_t launch_cs_stage(bool single, const double *segs, int n_seg,
-                            int Nx, int Ny, int Nz, double dx, double dz,
+__global__ void pivot_kernel(const double *__restrict__ segs, int n_seg,
+                             int Nx, int Ny, double dx, double dz, int row0,
+                             int n_rows, int nsteps, float4 *out) {
+    const long total = (long)n_rows * nsteps * n_seg;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total;
+         i += (long)gridDim.x * blockDim.x) {
+        const int s = (int)(i % n_seg);
+        const long t = i / n_seg;
+        const int k = (int)(t % nsteps);
+        const int r = (int)(t / nsteps);
+        const double y_pix = (row0 + r - Ny / 2) * dx;
+        out[i] = seg_pivot(segs + (size_t)s * DYFOX_SEG_STRIDE, y_pix, k * dz,
+                           Nx, dx);
+    }
+}
+
+cudaError_t launch_cs_stage(bool single, bool sum64, const double *segs,
+                            int n_seg, int Nx, int Ny, int Nz, double dx,
+                            double dz,
                             const VolterraConsts &vc, int row0, int n_rows,
                             void *out, cudaStream_t stream) {
     const int nsteps = Nz - 1;
@@ -138,17 +169,17 @@ cudaError_t launch_cs_stage(bool single, const double *segs, int n_seg,
     if (single) {
         size_t smem = (size_t)n_seg * sizeof(SegF) +
                       (size_t)kStageKB * n_seg * sizeof(float4) + sizeof(double);
+        auto *k = sum64 ? cs_stage_kernel<true, true> : cs_stage_kernel<true, false>;
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(
-                cs_stage_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                (int)smem);
+                k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
         }
-        cs_stage_kernel<true><<<(int)grid, 256, smem, stream>>>(
-            segs, n_seg, Nx, Ny, Nz, dx, dz, vc, row0, n_rows, out);
+        k<<<(int)grid, 256, smem, stream>>>(segs, n_seg, Nx, Ny, Nz, dx, dz,
+                                            vc, row0, n_rows, out);
         count_launch(1);
     } else {
-        cs_stage_kernel<false><<<(int)grid, 256, 0, stream>>>(
+        cs_stage_kernel<false, true><<<(int)grid, 256, 0, stream>>>(
             segs, n_seg, Nx, Ny, Nz, dx, dz, vc, row0, n_rows, out);
         count_launch(1);
     }
@@ -237,7 +268,7 @@ extern "C" int dyfox_segment_table(const double *segs, int n_seg,
             o[SEG_KQ] = -ge2 * b_perp / (4 * onu);
             o[SEG_HCONST] = o[SEG_KL] * log(dx * dx);
         }
-        o[SEG_DX] = dx;
+        o[SEG_C1] = b_perp / (2 * kPi);
         o[SEG_A2PX] = (a_core / dx) * (a_core / dx);
         o[SEG_SLOPE1] = e1[0] - xi[0] * dot3(xi, e1);
         o[SEG_SLOPE2] = e2[0] - xi[0] * dot3(xi, e2);

@@ -102,7 +102,7 @@ _MODES = {"auto": 0, "fused": _lib.FLAG_FUSED, "staged": _lib.FLAG_STAGED}
 
 def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
            pristine, h_mode="auto", compensated=True, general=False,
-           angles_per_cta=0, cols_per_lane=0, out=None):
+           angles_per_cta=0, cols_per_lane=0, out=None, h_sum="ff"):
     torch = _lib.torch_cuda()
     prec = as_precision(precision)
     s = np.atleast_1d(np.asarray(s_dev_arr, dtype=float))
@@ -115,6 +115,10 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
         flags |= _lib.FLAG_NO_COMP
     if general:
         flags |= _lib.FLAG_GENERAL
+    if h_sum not in ("ff", "fp64"):
+        raise ValueError(f"h_sum is 'ff' or 'fp64', not {h_sum!r}")
+    if h_sum == "fp64":
+        flags |= _lib.FLAG_H_FP64
     table_dev, n_seg, ap, H = None, 0, None, None
     if pristine:
         h_source = _lib.H_NONE
@@ -155,16 +159,18 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
 
 def solve_dislocation(seg_list, s_dev_arr, grid, xtal, *, H_gpu=None,
                       batch=64, precision=FP64, h_mode="auto",
-                      compensated=True):
+                      compensated=True, h_sum="ff"):
     """Exit wave of a dislocation field at each deviation parameter.
 
     ``batch`` caps the angles per launch (results do not depend on it).
     Keyword-only extensions: ``h_mode`` ("auto", "fused": H evaluated inside
     the march, "staged": e^{iH} computed once into the workspace and read by
-    every angle group), ``compensated`` (FP32 two-sum updates, default on).
+    every angle group), ``compensated`` (FP32 two-sum updates, default on),
+    ``h_sum`` (FP32: segment sum and 2 pi reduction in float-float "ff",
+    default, or in double "fp64").
     """
     return _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
-                  False, h_mode, compensated)
+                  False, h_mode, compensated, h_sum=h_sum)
 
 
 def solve_pristine(s_dev_arr, grid, xtal, *, precision=FP64):

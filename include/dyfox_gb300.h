@@ -36,8 +36,10 @@ typedef enum dyfox_status {
 
 /* Precision of a march.  FP64: plain double everywhere (parity mode).
  * FP32: single-precision march in the interaction picture with two-sum
- * compensated amplitude updates; H summed over segments and reduced mod
- * 2 pi in double; per-segment terms and sincos in single. */
+ * compensated amplitude updates; per-segment Volterra terms and sincos in
+ * single precision with offsets set up in double; the segment sum kept in
+ * float-float (two-sum) and reduced mod 2 pi exactly (Cody-Waite), or in
+ * double with DYFOX_FLAG_H_FP64. */
 #define DYFOX_FP64 0
 #define DYFOX_FP32 1
 
@@ -54,6 +56,9 @@ typedef enum dyfox_status {
 #define DYFOX_FLAG_NO_COMP 4u  /* FP32: plain (uncompensated) updates       */
 #define DYFOX_FLAG_GENERAL 8u  /* use the shared-memory general march even
                                   when shift_px == 1 (cross-checks)          */
+#define DYFOX_FLAG_H_FP64 16u  /* FP32 + H_SEGMENTS: sum the segment terms and
+                                  reduce mod 2 pi in double instead of in
+                                  float-float (two-sum) arithmetic           */
 
 /* Doubles per entry of a segment table (dyfox_segment_table). */
 #define DYFOX_SEG_STRIDE 24

@@ -216,8 +216,9 @@ def test_fp64_matches_the_reference_kernel_on_the_gpu(gpu, diamond400):
 
 
 @pytest.mark.parametrize("mode", ["fused", "staged"])
+@pytest.mark.parametrize("h_sum", ["ff", "fp64"])
 def test_fp32_compensated_meets_the_intensity_budget(gpu, diamond400, mode,
-                                                     rng):
+                                                     h_sum, rng):
     from dyfox_gb300.backend import FP32
     from dyfox_gb300.grid import LaueGrid
     from dyfox_gb300.laue import solve_dislocation
@@ -228,12 +229,12 @@ def test_fp32_compensated_meets_the_intensity_budget(gpu, diamond400, mode,
     s = deviation_from_urad([0.0, 117.5, -300.0, 30.0], diamond400)
     a = np_(solve_dislocation(seg, s, grid, diamond400, h_mode=mode))
     b = np_(solve_dislocation(seg, s, grid, diamond400, precision=FP32,
-                              h_mode=mode))
+                              h_mode=mode, h_sum=h_sum))
     assert b.dtype == np.complex64
     err = rel_l2(np.abs(b) ** 2, np.abs(a) ** 2)
     assert 0 < err < FP32_INTENSITY_TOL
     c = np_(solve_dislocation(seg, s, grid, diamond400, precision=FP32,
-                              h_mode=mode, compensated=False))
+                              h_mode=mode, compensated=False, h_sum=h_sum))
     assert rel_l2(np.abs(c) ** 2, np.abs(a) ** 2) < FP32_INTENSITY_TOL
 
 
@@ -250,16 +251,17 @@ def test_batching_does_not_change_the_scan(gpu, diamond400, small_grid):
     assert a.tobytes() == b.tobytes()
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec,h_sum", [("fp64", "ff"), ("fp32", "ff"),
+                                         ("fp32", "fp64")])
 def test_fused_and_staged_phase_agree_bitwise(gpu, diamond400, small_grid,
-                                             prec, rng):
+                                             prec, h_sum, rng):
     from dyfox_gb300.laue import solve_dislocation
     segs = random_segments(diamond400, small_grid, 4, rng)
     s = np.linspace(-3e5, 3e5, 5)
     a = np_(solve_dislocation(segs, s, small_grid, diamond400, precision=prec,
-                              h_mode="fused"))
+                              h_mode="fused", h_sum=h_sum))
     b = np_(solve_dislocation(segs, s, small_grid, diamond400, precision=prec,
-                              h_mode="staged"))
+                              h_mode="staged", h_sum=h_sum))
     assert a.tobytes() == b.tobytes()
 
 
