@@ -18,7 +18,10 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdyfox_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-              "--expt-relaxed-constexpr"]
+              "--expt-relaxed-constexpr",
+              # a declaration hiding an outer variable is an error (device
+              # and host code)
+              "-Xcudafe", "--diag_error=1348"]
 
 
 def nvcc():

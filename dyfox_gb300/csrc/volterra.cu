@@ -64,7 +64,8 @@ static int launch_h_rows(bool f32out, const double *segs, int n_seg, int Nx,
 // march over many deviation parameters (computed once, read by every angle
 // group).  One CTA per (row, KB steps).  Double: reference-order H and
 // sincos.  Single: pivot set-up per (row, step, segment) in double, segment
-// terms in single, their sum and the 2 pi reduction in double.
+// terms in single, their sum and the 2 pi reduction in float-float (or in
+// double when SUM64).
 constexpr int kStageKB = 4;
 
 template <bool SINGLE, bool SUM64>
@@ -99,12 +100,12 @@ __global__ void cs_stage_kernel(const double *__restrict__ segs, int n_seg,
         for (int j = tid; j < kn * Nx; j += nt) {
             const int kb = j / Nx, x = j - kb * Nx;
             const float4 *pv = piv + (size_t)kb * n_seg;
-            float r;
+            float ph;
             if (SUM64) {
                 double acc = hconst;
                 for (int s = 0; s < n_seg; ++s)
                     acc += (double)h_seg_f32(segf[s], pv[s], x);
-                r = reduce_2pi(acc);
+                ph = reduce_2pi(acc);
             } else {
                 float hi = hcr, lo = 0.0f;
                 for (int s = 0; s < n_seg; ++s) {
@@ -113,10 +114,10 @@ __global__ void cs_stage_kernel(const double *__restrict__ segs, int n_seg,
                     lo += (hi - (sum - bb)) + (h - bb);
                     hi = sum;
                 }
-                r = reduce_2pi_ff(hi, lo);
+                ph = reduce_2pi_ff(hi, lo);
             }
             float sn, c;
-            sincosf(r, &sn, &c);
+            sincosf(ph, &sn, &c);
             ((float2 *)out)[((size_t)r * nsteps + k0 + kb) * Nx + x] =
                 make_float2(c, sn);
         }
