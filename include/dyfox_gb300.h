@@ -112,6 +112,9 @@ typedef struct dyfox_laue_desc {
     int cols_per_lane;                       /* 0 = automatic              */
 } dyfox_laue_desc;
 
+/* Size of the fixed scratch array of dyfox_laue_solve_noalloc. */
+#define DYFOX_NOALLOC_SCRATCH_BYTES (32u << 20)
+
 /* Workspace bytes dyfox_laue_solve needs for this descriptor. */
 size_t dyfox_laue_workspace_bytes(const dyfox_laue_desc *d);
 
@@ -128,6 +131,25 @@ size_t dyfox_laue_workspace_bytes(const dyfox_laue_desc *d);
 int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
                      const void *h_grid, const double *seg_table, void *out,
                      void *workspace, size_t workspace_bytes, void *stream);
+
+/* dyfox_laue_solve for callers that cannot allocate device memory when
+ * they solve (no counterpart in the DYFOX reference).  Examples: a real-time
+ * acquisition or reconstruction loop that reserves its device memory once
+ * and must not fail on an allocation mid-run, a plugin host that forbids
+ * allocations after start-up, or a C/Fortran caller with no device
+ * allocator of its own.  Same arguments and results as dyfox_laue_solve,
+ * without the workspace: the scratch is a fixed array of
+ * DYFOX_NOALLOC_SCRATCH_BYTES (32 MiB) in the library's device memory, held
+ * by every GPU that loads the library until the process exits.  Problems
+ * whose dyfox_laue_workspace_bytes exceeds it return DYFOX_ENOMEM.  The
+ * first call on each device looks the array's address up with that device
+ * current (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the array, which keeps the last call's contents
+ * (nothing in it has to start at zero); calls whose work overlaps on the GPU
+ * race on it and must be serialised.  Allocates no device memory. */
+int dyfox_laue_solve_noalloc(const dyfox_laue_desc *d, const double *s_dev,
+                             const void *h_grid, const double *seg_table,
+                             void *out, void *stream);
 
 typedef struct dyfox_bragg_desc {
     double sig0[2], sig_h[2], sig_hbar[2];   /* (re, im), 1/m              */
