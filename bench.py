@@ -58,43 +58,18 @@ def parse():
                     help="run one solve of that form after one warm-up and "
                          "exit (a small, fixed case for ncu)")
     ap.add_argument("--no-bragg", action="store_true")
+    ap.add_argument("--no-scan", action="store_true")
     return ap.parse_args()
 
 
 def workload():
-    from dyfox_gb300.crystal import diamond_400
-    from dyfox_gb300.dislocations import burgers_vector, straight_segment
-    from dyfox_gb300.grid import LaueGrid
-    from dyfox_gb300.units import deviation_from_urad
-    x = diamond_400()
-    grid = LaueGrid(x, t_crystal=200e-6, dx=0.25e-6, beam_width=120e-6)
-    b = burgers_vector(x.U_lab, [1, 0, -1], x.b_mag, +1)
-    z0 = grid.t_crystal / 2
-    seg = straight_segment(np.array([1.0, 0.0, 1.0]) / np.sqrt(2.0), b,
-                           [-z0 * x.tan_tB, grid.dx / 2, z0], 800e-6)
-    s = deviation_from_urad([0.0, 117.5], x)
-    return x, grid, seg, s
+    from dyfox_gb300.workloads import laue_readme
+    return laue_readme()
 
 
 def bragg_workload():
-    """Bragg config 1: diamond (400) 17 keV, t = 20 um, dx = 0.5 um,
-    half_x = 16 um (Nz = 90, Nx = 456), 64 y-planes, 21 deviation parameters
-    evenly over +-3 Darwin widths, one edge dislocation (line [101],
-    b = (a/2)[10-1]) through the column at depth t/2, tol 1e-10."""
-    from dyfox_gb300.bragg_geometry import (BraggConfig, bragg_g_vector,
-                                            darwin_width_urad)
-    from dyfox_gb300.crystal import diamond_400
-    from dyfox_gb300.dislocations import burgers_vector, straight_segment
-    from dyfox_gb300.units import deviation_from_urad
-    x = diamond_400()
-    cfg = BraggConfig(x, t_crystal=20e-6, dx=0.5e-6, half_x=16e-6)
-    b = burgers_vector(np.eye(3), [1, 0, -1], x.b_mag, +1)
-    seg = straight_segment(np.array([1.0, 0.0, 1.0]) / np.sqrt(2.0), b,
-                           [0.0, 0.0, cfg.t_crystal / 2], 800e-6)
-    w = darwin_width_urad(x)
-    s = deviation_from_urad(np.linspace(-3 * w, 3 * w, 21), x)
-    ys = (np.arange(64) - 32 + 0.5) * cfg.dx
-    return x, cfg, seg, s, ys, bragg_g_vector(x)
+    from dyfox_gb300.workloads import bragg_config1
+    return bragg_config1()
 
 
 def active_rows(geo):
@@ -357,12 +332,71 @@ def run_ours(args):
     line["clocks"] = clk_sum
     if not args.no_bragg:
         line["bragg"] = bragg_leg(args, rank, world)
+    if not args.no_scan:
+        line["laue_scan"] = scan_leg(args, world)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, grid, seg, s, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def scan_leg(args, world):
+    """The 256-angle rocking scan (t = 273 um, 544 x 1056, Nz 490, 64 random
+    <110> segments): chosen FP32 form, e^{iH} staged once (float-float
+    segment sum) and read by every angle group.  Accuracy is checked
+    against plain FP64 on 8 of the 256 angles."""
+    import torch
+    from dyfox_gb300 import _lib
+    from dyfox_gb300.grid import grid_arrays
+    from dyfox_gb300.laue import solve_dislocation
+    from dyfox_gb300.workloads import laue_rocking_scan
+    x, grid, segs, s = laue_rocking_scan()
+    geo = grid_arrays(grid)
+    rows = active_rows(geo)
+    units = len(s) * len(rows) * geo["Nx"] * (geo["Nz"] - 1)
+    stream = torch.cuda.current_stream()
+    L = _lib.lib()
+    out = torch.empty((len(s), geo["Ny"], geo["Nx"]), dtype=torch.complex64,
+                      device="cuda")
+    for _ in range(2):
+        solve_dislocation(segs, s, grid, x, precision="fp32",
+                          h_mode="staged", batch=len(s))
+    torch.cuda.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    times = []
+    n0 = L.dyfox_launch_count()
+    steps = max(3, args.steps // 4)
+    for _ in range(steps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = solve_dislocation(segs, s, grid, x, precision="fp32",
+                                h_mode="staged", batch=len(s))
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    launches = L.dyfox_launch_count() - n0
+    pick = np.linspace(0, len(s) - 1, 8).round().astype(int)
+    t0 = time.perf_counter()
+    ref = solve_dislocation(segs, s[pick], grid, x, precision="fp64")
+    torch.cuda.synchronize()
+    fp64_s = time.perf_counter() - t0
+    I32 = out[torch.as_tensor(pick, device="cuda")].abs().double() ** 2
+    I64 = ref.abs() ** 2
+    err = float(torch.linalg.vector_norm(I32 - I64)
+                / torch.linalg.vector_norm(I64))
+    ms = statistics.mean(times)
+    return {"value": world * units / (ms * 1e-3), "unit": "voxel-steps/s",
+            "ms_per_scan": ms, "voxel_steps_per_scan": units,
+            "angles": len(s), "segments": len(segs), "active_rows":
+            int(len(rows)), "Nx": geo["Nx"], "Nz": geo["Nz"],
+            "form": "FP32 compensated march, e^{iH} staged once "
+                    "(float-float segment sum), all angles in one call",
+            "intensity_rel_l2_vs_fp64_8_angles": err,
+            "fp64_8_angles_s": fp64_s, "gpu_launches": int(launches)}
 
 
 def bragg_leg(args, rank, world):

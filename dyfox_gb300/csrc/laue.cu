@@ -27,7 +27,7 @@ __global__ void laue_setup_kernel(const double *__restrict__ s_dev, int n_e,
                                   int nsteps, double ds, double s0r,
                                   double s0i, double shr, double shi,
                                   double sbr, double sbi, Kappa *kappa,
-                                  double2 *scale) {
+                                  float4 *kappa32, double2 *scale) {
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (idx >= (long)n_e * nsteps) return;
     const int ie = (int)(idx / nsteps), k = (int)(idx - (long)ie * nsteps);
@@ -57,6 +57,8 @@ __global__ void laue_setup_kernel(const double *__restrict__ s_dev, int n_e,
     kp.k12 = make_double2(f * (sbr * wr - sbi * wi), f * (sbr * wi + sbi * wr));
     kp.k21 = make_double2(f * (shr * wr + shi * wi), f * (shi * wr - shr * wi));
     kappa[idx] = kp;
+    kappa32[idx] = make_float4((float)kp.k12.x, (float)kp.k12.y,
+                               (float)kp.k21.x, (float)kp.k21.y);
     if (k == 0) {
         const double exp_pr = exp(s0r * ds);
         const double pi_ = (s0i + alpha * 0.5) * ds;
@@ -202,7 +204,8 @@ struct LauePlan {
     int hsrc = HS_NONE;      // source the march kernel reads
     int stage = 0;           // 0: none, 1: stage e^{iH} (CS32/CS64)
     int row0 = 0, n_rows = 0;
-    size_t off_kappa = 0, off_scale = 0, off_stage = 0, off_piv = 0, ws = 0;
+    size_t off_kappa = 0, off_k32 = 0, off_scale = 0, off_stage = 0,
+           off_piv = 0, ws = 0;
 };
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -280,6 +283,8 @@ static int make_plan(const dyfox_laue_desc *d, LauePlan *p) {
     size_t off = 0;
     p->off_kappa = off;
     off = align256(off + (size_t)d->n_e * (d->Nz - 1) * sizeof(Kappa));
+    p->off_k32 = off;
+    off = align256(off + (size_t)d->n_e * (d->Nz - 1) * sizeof(float4));
     p->off_scale = off;
     off = align256(off + (size_t)d->n_e * sizeof(double2));
     p->off_stage = off;
@@ -434,6 +439,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     a.vc = volterra_consts(d->nu, d->a_core);
     memcpy(a.an, d->analytic, sizeof a.an);
     a.kappa = (const Kappa *)(ws + p.off_kappa);
+    a.kappa32 = (const float4 *)(ws + p.off_k32);
     a.scale = (const double2 *)(ws + p.off_scale);
     a.out = out;
     a.csgrid = ws + p.off_stage;
@@ -457,7 +463,8 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
         laue_setup_kernel<<<(int)((n + 255) / 256), 256, 0, stream>>>(
             s_dev, d->n_e, nsteps, d->ds, d->sig0[0], d->sig0[1], d->sig_h[0],
             d->sig_h[1], d->sig_hbar[0], d->sig_hbar[1],
-            (Kappa *)(ws + p.off_kappa), (double2 *)(ws + p.off_scale));
+            (Kappa *)(ws + p.off_kappa), (float4 *)(ws + p.off_k32),
+            (double2 *)(ws + p.off_scale));
         count_launch(1);
         if ((e = cudaGetLastError())) return cuda_status(e, "laue_setup");
     }

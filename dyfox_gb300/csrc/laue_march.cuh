@@ -66,6 +66,7 @@ struct MarchArgs {
     VolterraConsts vc;
     double an[12];              // ANALYTIC
     const Kappa *kappa;         // (n_e, Nz - 1): kappa12, kappa21
+    const float4 *kappa32;      // the same, rounded to float (FP32 march)
     const double2 *scale;       // (n_e): M22^(Nz-1)
     void *out;                  // (n_e, Ny, Nx) complex (R2)
 };
@@ -330,16 +331,25 @@ __global__ void laue_march_kernel(const MarchArgs a) {
     __syncthreads();
 
     const Kappa *kap = a.kappa + (size_t)ie * nsteps;
-    Kappa kn = ldg_kappa(kap);
+    const float4 *kap32 = a.kappa32 + (size_t)ie * nsteps;
+    Kappa kn;
+    float4 kn32;
+    if constexpr (kSingle) kn32 = __ldg(kap32);
+    else kn = ldg_kappa(kap);
     // ------------------------------------------------------------ march
     for (int k = 0; k < nsteps; ++k) {
         const int p = k & 1;
-        const Kappa kk4 = kn;
-        if (k + 1 < nsteps) kn = ldg_kappa(kap + k + 1);
+        R k12r, k12i, k21r, k21i;
+        if constexpr (kSingle) {
+            k12r = kn32.x; k12i = kn32.y; k21r = kn32.z; k21i = kn32.w;
+            if (k + 1 < nsteps) kn32 = __ldg(kap32 + k + 1);
+        } else {
+            k12r = (R)kn.k12.x; k12i = (R)kn.k12.y;
+            k21r = (R)kn.k21.x; k21i = (R)kn.k21.y;
+            if (k + 1 < nsteps) kn = ldg_kappa(kap + k + 1);
+        }
         if (k + 1 < nsteps) produce(k + 1, p ^ 1);
 
-        const R k12r = (R)kk4.k12.x, k12i = (R)kk4.k12.y;
-        const R k21r = (R)kk4.k21.x, k21i = (R)kk4.k21.y;
         // Neighbour values of the previous state.
         R ainr = __shfl_down_sync(0xffffffffu, Ar[0], 1);
         R aini = __shfl_down_sync(0xffffffffu, Ai[0], 1);

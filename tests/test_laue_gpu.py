@@ -357,3 +357,17 @@ def test_bad_inputs_raise(gpu, diamond400, small_grid):
         solve_dislocation([], [0.0], small_grid, diamond400,
                           H_gpu=torch.zeros(3, 3, 3, device="cuda",
                                             dtype=torch.float64))
+
+
+def test_rocking_scan_configuration_meets_the_budget(gpu, diamond400):
+    """The 273 um, 64-segment scan configuration on 8 of its angles: FP32
+    compensated (staged and fused phase) against plain FP64."""
+    from dyfox_gb300.laue import solve_dislocation
+    from dyfox_gb300.workloads import laue_rocking_scan
+    x, grid, segs, s = laue_rocking_scan(n_angles=8)
+    assert len(segs) == 64
+    a = np_(solve_dislocation(segs, s, grid, x, precision="fp64"))
+    for mode in ("staged", "fused"):
+        b = np_(solve_dislocation(segs, s, grid, x, precision="fp32",
+                                  h_mode=mode))
+        assert rel_l2(np.abs(b) ** 2, np.abs(a) ** 2) < FP32_INTENSITY_TOL
