@@ -54,11 +54,14 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--once", choices=["fp32", "fp64", "bragg"],
+    ap.add_argument("--once", choices=["fp32", "fp64", "bragg", "scan"],
                     help="run one solve of that form after one warm-up and "
                          "exit (a small, fixed case for ncu)")
     ap.add_argument("--no-bragg", action="store_true")
     ap.add_argument("--no-scan", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the launch-shape autotuner (use its cache or "
+                         "the built-in choice)")
     return ap.parse_args()
 
 
@@ -174,9 +177,20 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     sp = _lib.c_void_p(stream.cuda_stream)
 
+    from dyfox_gb300.autotune import lookup, tune
+    tuned = {}
+    if not args.no_tune and not args.once:
+        for name, prec in (("fp32", FP32), ("fp64", FP64)):
+            r = tune(seg, s, grid, x, precision=prec, h_mode="fused")
+            tuned[name] = {"cols_per_lane": r["cols_per_lane"],
+                           "angles_per_cta": r["angles_per_cta"]}
+
     def make(prec, extra=0):
         d = _desc(x, geo, n_e, prec, _lib.H_SEGMENTS, len(table),
                   flags=_lib.FLAG_FUSED | extra)
+        shape = lookup(d)
+        if shape is not None:
+            d.cols_per_lane, d.angles_per_cta = shape
         nb = L.dyfox_laue_workspace_bytes(d)
         ws = torch.empty(max(nb, 256), dtype=torch.uint8, device="cuda")
         out = torch.empty((n_e, geo["Ny"], geo["Nx"]),
@@ -197,6 +211,14 @@ def run_ours(args):
         torch.cuda.synchronize()
         fn()
         torch.cuda.synchronize()
+        return
+    if args.once == "scan":
+        from dyfox_gb300.workloads import laue_rocking_scan
+        sx, sgrid, ssegs, ss = laue_rocking_scan(n_angles=32)
+        for _ in range(2):
+            solve_dislocation(ssegs, ss, sgrid, sx, precision="fp32",
+                              h_mode="staged", batch=len(ss))
+            torch.cuda.synchronize()
         return
     if args.once == "bragg":
         from dyfox_gb300.bragg import solve_scan
@@ -325,6 +347,9 @@ def run_ours(args):
                                     "(dyfox_pipe_peak, this run)",
                      "algorithmic_flops_per_launch": flops},
         "pipe_peaks_tflops": peaks,
+        "launch_shape": {"tuned": tuned or None,
+                         "autotuner": "dyfox_gb300.autotune (cols per lane x "
+                                      "angles per CTA, timed on 32 rows)"},
         "gpu_launches": int(launches),
         "wall_s": wall,
     }
@@ -358,8 +383,12 @@ def scan_leg(args, world):
     units = len(s) * len(rows) * geo["Nx"] * (geo["Nz"] - 1)
     stream = torch.cuda.current_stream()
     L = _lib.lib()
-    out = torch.empty((len(s), geo["Ny"], geo["Nx"]), dtype=torch.complex64,
-                      device="cuda")
+    shape = None
+    if not args.no_tune:
+        from dyfox_gb300.autotune import tune
+        r = tune(segs, s, grid, x, precision="fp32", h_mode="staged")
+        shape = {"cols_per_lane": r["cols_per_lane"],
+                 "angles_per_cta": r["angles_per_cta"]}
     for _ in range(2):
         solve_dislocation(segs, s, grid, x, precision="fp32",
                           h_mode="staged", batch=len(s))
@@ -396,7 +425,8 @@ def scan_leg(args, world):
             "form": "FP32 compensated march, e^{iH} staged once "
                     "(float-float segment sum), all angles in one call",
             "intensity_rel_l2_vs_fp64_8_angles": err,
-            "fp64_8_angles_s": fp64_s, "gpu_launches": int(launches)}
+            "fp64_8_angles_s": fp64_s, "gpu_launches": int(launches),
+            "launch_shape": shape}
 
 
 def bragg_leg(args, rank, world):

@@ -1,0 +1,134 @@
+"""Launch-shape autotuner of the Laue march.
+
+The register-resident march has two free shape parameters: columns per lane
+(CPL, the register tile of one thread: 4-8 in FP64, 5-13 in FP32) and
+angles per CTA (how many deviation parameters share one e^{iH} row, each
+with WA = ceil(Nx / (32 CPL)) warps).  The best pair depends on Nx, on the
+number of angles, on the H source and on the precision.  ``tune`` times the
+candidates on a copy of the grid cut down to a few rows (same Nx and Nz, so
+the per-row work is unchanged), keeps the fastest, and caches it per GPU
+model and problem signature in a JSON file (``DYFOX_TUNE_CACHE``, default
+``~/.cache/dyfox_gb300/laue_tune.json``).  ``solve_dislocation`` and
+``solve_pristine`` read the cache for every solve whose shape is not given
+explicitly.
+"""
+
+import json
+import os
+import threading
+
+import numpy as np
+
+from . import _lib
+
+CPL = {"fp64": (4, 5, 6, 7, 8), "fp32": (5, 7, 9, 11, 13)}
+ANGLES = (1, 2, 3, 4, 6, 8)
+_lock = threading.Lock()
+_cache = None
+
+
+def cache_path():
+    return os.environ.get("DYFOX_TUNE_CACHE", os.path.join(
+        os.path.expanduser("~"), ".cache", "dyfox_gb300", "laue_tune.json"))
+
+
+def _load():
+    global _cache
+    if _cache is None:
+        try:
+            with open(cache_path()) as f:
+                _cache = json.load(f)
+        except (OSError, ValueError):
+            _cache = {}
+    return _cache
+
+
+def _save():
+    path = cache_path()
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(_cache, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def _bucket(n):
+    """Angle counts are bucketed by powers of two above 8 (the shape that
+    is best for 200 angles is best for 256)."""
+    if n <= 8:
+        return n
+    return 1 << int(np.ceil(np.log2(n)))
+
+
+def signature(desc):
+    torch = _lib.torch_cuda()
+    name = torch.cuda.get_device_name()
+    return "|".join(str(v) for v in (
+        name, desc.precision, desc.h_source, desc.flags & ~_lib.FLAG_GENERAL,
+        desc.Nx, desc.Nz, _bucket(desc.n_e), _bucket(desc.n_seg)))
+
+
+def lookup(desc):
+    """(cols_per_lane, angles_per_cta) cached for this signature, or None."""
+    with _lock:
+        e = _load().get(signature(desc))
+    return None if e is None else (e["cols_per_lane"], e["angles_per_cta"])
+
+
+def tune(seg_list, s_dev_arr, grid, xtal, *, precision="fp32",
+         h_mode="auto", H_gpu=None, compensated=True, h_sum="ff", rows=32,
+         repeats=3, verbose=False):
+    """Time every (CPL, angles per CTA) candidate for this problem and cache
+    the fastest.  Returns {"cols_per_lane", "angles_per_cta", "ms",
+    "candidates": [(cpl, A, ms), ...]}."""
+    from .backend import precision as as_precision
+    from .grid import grid_arrays
+    from .laue import _solve
+    torch = _lib.torch_cuda()
+    prec = as_precision(precision)
+    small = grid.replace(beam_width=rows * grid.dx) if H_gpu is None else grid
+    s = np.atleast_1d(np.asarray(s_dev_arr, float))
+    geo = grid_arrays(small)
+    results = []
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), \
+        torch.cuda.Event(enable_timing=True)
+    out = torch.empty((len(s), geo["Ny"], geo["Nx"]), dtype=prec.torch_complex,
+                      device="cuda")
+    for cpl in CPL[prec.name]:
+        if -(-geo["Nx"] // (32 * cpl)) > 32:
+            continue
+        for A in ANGLES:
+            if A > len(s):
+                continue
+            try:
+                kw = dict(h_mode=h_mode, angles_per_cta=A, cols_per_lane=cpl,
+                          out=out, tuned=False, compensated=compensated,
+                          h_sum=h_sum)
+                _solve(seg_list, s, small, xtal, H_gpu, 0, prec, False, **kw)
+                torch.cuda.synchronize()
+                best = np.inf
+                for _ in range(repeats):
+                    ev0.record()
+                    _solve(seg_list, s, small, xtal, H_gpu, 0, prec, False,
+                           **kw)
+                    ev1.record()
+                    torch.cuda.synchronize()
+                    best = min(best, ev0.elapsed_time(ev1))
+            except (ValueError, NotImplementedError, MemoryError):
+                continue
+            results.append((cpl, A, best))
+            if verbose:
+                print(f"cpl {cpl:2d} angles/CTA {A}: {best:.3f} ms")
+    if not results:
+        raise RuntimeError("no launch shape could run this problem")
+    cpl, A, ms = min(results, key=lambda r: r[2])
+    from .laue import describe
+    d = describe(seg_list, s, grid, xtal, H_gpu=H_gpu, precision=prec,
+                 h_mode=h_mode, compensated=compensated, h_sum=h_sum)
+    with _lock:
+        _load()[signature(d)] = {"cols_per_lane": cpl, "angles_per_cta": A,
+                                 "ms_reduced_rows": ms, "rows": rows}
+        _save()
+    return {"cols_per_lane": cpl, "angles_per_cta": A, "ms": ms,
+            "candidates": results}
+

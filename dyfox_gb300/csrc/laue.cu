@@ -257,6 +257,24 @@ static void active_rows(const dyfox_laue_desc *d, int *row0, int *n_rows) {
     *n_rows = count;
 }
 
+// Angles one CTA of the register-resident march holds at this Nx: fusing
+// the Volterra phase into the march pays only when every angle of a row
+// shares one evaluation, i.e. one CTA holds them all.
+static int fused_angle_limit(const dyfox_laue_desc *d) {
+    const bool single = d->precision == DYFOX_FP32;
+    const int *cpls = single ? kCplF32 : kCplF64;
+    const int ncpl = single ? kNumCplF32 : kNumCplF64;
+    int best = 1 << 30;
+    for (int i = 0; i < ncpl; ++i) {
+        if (d->cols_per_lane && cpls[i] != d->cols_per_lane) continue;
+        const int wa = div_up(d->Nx, 32 * cpls[i]);
+        if (wa <= 16 && wa < best) best = wa;
+    }
+    if (best == 1 << 30) return 1;
+    const int a = 512 / (32 * best);
+    return a < 8 ? (a < 1 ? 1 : a) : 8;
+}
+
 static int make_plan(const dyfox_laue_desc *d, LauePlan *p) {
     int st = validate(d);
     if (st) return st;
@@ -273,7 +291,7 @@ static int make_plan(const dyfox_laue_desc *d, LauePlan *p) {
         bool fused;
         if (d->flags & DYFOX_FLAG_FUSED) fused = true;
         else if (d->flags & DYFOX_FLAG_STAGED) fused = false;
-        else fused = d->n_e <= 8;   // one CTA can hold every angle
+        else fused = d->n_e <= fused_angle_limit(d);
         if (p->general) fused = false;
         if (d->n_seg == 0) { p->hsrc = HS_NONE; break; }
         p->hsrc = fused ? HS_SEG : (single ? HS_CS32 : HS_CS64);

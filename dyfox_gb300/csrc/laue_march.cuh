@@ -119,7 +119,7 @@ template <> struct CS<double> {
 template <> struct CS<float> {
     static __device__ __forceinline__ float2 of_f64(double h) {
         float s, c;
-        sincosf(reduce_2pi(h), &s, &c);
+        __sincosf(reduce_2pi(h), &s, &c);     // argument within [-pi, pi]
         return make_float2(c, s);
     }
     static __device__ __forceinline__ float2 of_f32(float h) {
@@ -252,7 +252,7 @@ __global__ void laue_march_kernel(const MarchArgs a) {
                             lo += e;
                         }
                         float sn, c;
-                        sincosf(reduce_2pi_ff(hi, lo), &sn, &c);
+                        __sincosf(reduce_2pi_ff(hi, lo), &sn, &c);
                         v.x = c;
                         v.y = sn;
                     } else {

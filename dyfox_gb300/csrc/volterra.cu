@@ -117,7 +117,7 @@ __global__ void cs_stage_kernel(const double *__restrict__ segs, int n_seg,
                 ph = reduce_2pi_ff(hi, lo);
             }
             float sn, c;
-            sincosf(ph, &sn, &c);
+            __sincosf(ph, &sn, &c);           // ph within [-pi, pi]
             ((float2 *)out)[((size_t)r * nsteps + k0 + kb) * Nx + x] =
                 make_float2(c, sn);
         }

@@ -100,16 +100,22 @@ def _desc(xtal, geo, n_e, prec, h_source, n_seg=0, analytic=None, flags=0,
 _MODES = {"auto": 0, "fused": _lib.FLAG_FUSED, "staged": _lib.FLAG_STAGED}
 
 
-def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
-           pristine, h_mode="auto", compensated=True, general=False,
-           angles_per_cta=0, cols_per_lane=0, out=None, h_sum="ff"):
-    torch = _lib.torch_cuda()
-    prec = as_precision(precision)
-    s = np.atleast_1d(np.asarray(s_dev_arr, dtype=float))
-    geo = grid_arrays(grid)
-    _check_angles(s, xtal, geo)
-    Nx, Ny, Nz = geo["Nx"], geo["Ny"], geo["Nz"]
-    n_e = len(s)
+def _h_source_of(seg_list, xtal, H_gpu, pristine=False):
+    """The C ABI's H source for these inputs (no device work)."""
+    if pristine:
+        return _lib.H_NONE
+    if H_gpu is not None:
+        torch = _lib.torch_cuda()
+        dt = H_gpu.dtype if isinstance(H_gpu, torch.Tensor) else None
+        return _lib.H_GRID_F32 if dt == torch.float32 else _lib.H_GRID_F64
+    if analytic_line_params(seg_list, xtal) is not None:
+        return _lib.H_ANALYTIC
+    return _lib.H_SEGMENTS
+
+
+def _flags(prec, h_mode, compensated, general, h_sum):
+    if h_mode not in _MODES:
+        raise ValueError(f"h_mode is one of {sorted(_MODES)}, not {h_mode!r}")
     flags = _MODES[h_mode]
     if prec.is_fp32 and not compensated:
         flags |= _lib.FLAG_NO_COMP
@@ -119,23 +125,34 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
         raise ValueError(f"h_sum is 'ff' or 'fp64', not {h_sum!r}")
     if h_sum == "fp64":
         flags |= _lib.FLAG_H_FP64
+    return flags
+
+
+def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
+           pristine, h_mode="auto", compensated=True, general=False,
+           angles_per_cta=0, cols_per_lane=0, out=None, h_sum="ff",
+           tuned=True):
+    torch = _lib.torch_cuda()
+    prec = as_precision(precision)
+    s = np.atleast_1d(np.asarray(s_dev_arr, dtype=float))
+    geo = grid_arrays(grid)
+    _check_angles(s, xtal, geo)
+    Nx, Ny, Nz = geo["Nx"], geo["Ny"], geo["Nz"]
+    n_e = len(s)
+    flags = _flags(prec, h_mode, compensated, general, h_sum)
     table_dev, n_seg, ap, H = None, 0, None, None
-    if pristine:
-        h_source = _lib.H_NONE
-    elif H_gpu is not None:
+    h_source = _h_source_of(seg_list, xtal, H_gpu, pristine)
+    if h_source in (_lib.H_GRID_F64, _lib.H_GRID_F32):
         H = _as_device_grid(H_gpu, Ny, Nz, Nx)
         h_source = (_lib.H_GRID_F64 if H.dtype == torch.float64
                     else _lib.H_GRID_F32)
-    else:
+    elif h_source == _lib.H_ANALYTIC:
         ap = analytic_line_params(seg_list, xtal)
-        if ap is not None:
-            h_source = _lib.H_ANALYTIC
-        else:
-            h_source = _lib.H_SEGMENTS
-            table = _lib.segment_table(seg_list, xtal.g_vec, xtal.nu,
-                                       xtal.a_core, geo["dx"])
-            n_seg = len(table)
-            table_dev = _lib.device_table(table)
+    elif h_source == _lib.H_SEGMENTS:
+        table = _lib.segment_table(seg_list, xtal.g_vec, xtal.nu,
+                                   xtal.a_core, geo["dx"])
+        n_seg = len(table)
+        table_dev = _lib.device_table(table)
     if out is None:
         out = torch.empty((n_e, Ny, Nx), dtype=prec.torch_complex,
                           device="cuda")
@@ -146,6 +163,11 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
         be = min(bs + batch, n_e)
         d = _desc(xtal, geo, be - bs, prec, h_source, n_seg, ap, flags,
                   angles_per_cta, cols_per_lane)
+        if tuned and not angles_per_cta and not cols_per_lane:
+            from .autotune import lookup
+            shape = lookup(d)
+            if shape is not None:
+                d.cols_per_lane, d.angles_per_cta = shape
         nbytes = _lib.lib().dyfox_laue_workspace_bytes(d)
         if nbytes == 0:
             _lib.check(_lib.DYFOX_EINVAL, "dyfox_laue_workspace_bytes")
@@ -155,6 +177,23 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
             _lib.ptr(table_dev), _lib.c_void_p(out[bs].data_ptr()),
             _lib.ptr(ws), ws.numel(), stream), "dyfox_laue_solve")
     return out
+
+
+def describe(seg_list, s_dev_arr, grid, xtal, *, H_gpu=None,
+             precision=FP64, h_mode="auto", compensated=True, h_sum="ff"):
+    """The C-ABI descriptor one solve_dislocation call would use (host only;
+    the autotuner keys its cache on it)."""
+    prec = as_precision(precision)
+    s = np.atleast_1d(np.asarray(s_dev_arr, dtype=float))
+    h_source = _h_source_of(seg_list, xtal, H_gpu)
+    n_seg = 0
+    if h_source == _lib.H_SEGMENTS:
+        n_seg = len(_lib.segment_table(seg_list, xtal.g_vec, xtal.nu,
+                                       xtal.a_core, grid.dx))
+    ap = analytic_line_params(seg_list, xtal) \
+        if h_source == _lib.H_ANALYTIC else None
+    return _desc(xtal, grid_arrays(grid), len(s), prec, h_source, n_seg, ap,
+                 _flags(prec, h_mode, compensated, False, h_sum))
 
 
 def solve_dislocation(seg_list, s_dev_arr, grid, xtal, *, H_gpu=None,

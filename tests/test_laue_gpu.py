@@ -371,3 +371,28 @@ def test_rocking_scan_configuration_meets_the_budget(gpu, diamond400):
         b = np_(solve_dislocation(segs, s, grid, x, precision="fp32",
                                   h_mode=mode))
         assert rel_l2(np.abs(b) ** 2, np.abs(a) ** 2) < FP32_INTENSITY_TOL
+
+
+def test_autotuner_caches_a_shape_that_changes_nothing(gpu, diamond400,
+                                                      small_grid, tmp_path,
+                                                      monkeypatch):
+    """The tuner times (columns per lane, angles per CTA) candidates, caches
+    the fastest, and solves read the cache; the shape never changes a bit
+    of the result."""
+    from dyfox_gb300 import autotune
+    from dyfox_gb300.laue import describe, solve_dislocation
+    monkeypatch.setenv("DYFOX_TUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_cache", None)
+    seg = geometry_n(diamond400, small_grid)
+    s = np.linspace(-3e5, 3e5, 3)
+    before = np_(solve_dislocation(seg, s, small_grid, diamond400,
+                                   precision="fp32"))
+    r = autotune.tune(seg, s, small_grid, diamond400, precision="fp32",
+                      rows=8)
+    assert len(r["candidates"]) >= 2
+    assert (tmp_path / "tune.json").exists()
+    d = describe(seg, s, small_grid, diamond400, precision="fp32")
+    assert autotune.lookup(d) == (r["cols_per_lane"], r["angles_per_cta"])
+    after = np_(solve_dislocation(seg, s, small_grid, diamond400,
+                                  precision="fp32"))
+    assert before.tobytes() == after.tobytes()

@@ -195,3 +195,32 @@ def test_bragg_oracle_solutions_match_the_reference(diamond400):
     out, info = BO.solve_surface(seg, s, cfg, b["ys"], diamond400, g)
     assert info["converged"]
     assert rel_l2(out, b["surface"]) < 1e-8
+
+
+def test_single_precision_atan2_polynomial():
+    """The polynomial of atan2_fast (csrc/volterra.cuh), evaluated in float32
+    with the same octant folding, against numpy.arctan2."""
+    import importlib.util
+    import os
+    from conftest import ROOT
+    spec = importlib.util.spec_from_file_location(
+        "fit_atan", os.path.join(ROOT, "dyfox_gb300", "csrc", "fit_atan.py"))
+    fa = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(fa)
+    c = np.array([0.9999993443489075, -0.33329859375953674,
+                  0.19946564733982086, -0.1390862762928009,
+                  0.09642191231250763, -0.05591224133968353,
+                  0.021862896159291267, -0.004054549150168896], np.float32)
+    np.testing.assert_allclose(fa.fit(), c, rtol=1e-5, atol=1e-7)
+    rng = np.random.default_rng(1)
+    y = (rng.normal(size=200000) * 10 ** rng.uniform(-3, 3, 200000)).astype(
+        np.float32)
+    x = (rng.normal(size=200000) * 10 ** rng.uniform(-3, 3, 200000)).astype(
+        np.float32)
+    ax, ay = np.abs(x), np.abs(y)
+    t = np.minimum(ax, ay) / np.maximum(ax, ay)
+    r = fa.eval_f32(c, t).astype(np.float64)
+    r = np.where(ay > ax, np.pi / 2 - r, r)
+    r = np.where(x < 0, np.pi - r, r)
+    r = np.copysign(r, y)
+    assert np.abs(r - np.arctan2(y.astype(float), x.astype(float))).max() < 3e-7
