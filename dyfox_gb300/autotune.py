@@ -5,8 +5,10 @@ The register-resident march has two free shape parameters: columns per lane
 angles per CTA (how many deviation parameters share one e^{iH} row, each
 with WA = ceil(Nx / (32 CPL)) warps).  The best pair depends on Nx, on the
 number of angles, on the H source and on the precision.  ``tune`` times the
-candidates on a copy of the grid cut down to a few rows (same Nx and Nz, so
-the per-row work is unchanged), keeps the fastest, and caches it per GPU
+candidates on a copy of the grid cut down in rows (same Nx and Nz, so the
+per-row work is unchanged) but with about 2048 CTAs per candidate, enough to
+fill the GPU as the full problem does, compares time per row, keeps the
+fastest, and caches it per GPU
 model and problem signature in a JSON file (``DYFOX_TUNE_CACHE``, default
 ``~/.cache/dyfox_gb300/laue_tune.json``).  ``solve_dislocation`` and
 ``solve_pristine`` read the cache for every solve whose shape is not given
@@ -76,7 +78,7 @@ def lookup(desc):
 
 
 def tune(seg_list, s_dev_arr, grid, xtal, *, precision="fp32",
-         h_mode="auto", H_gpu=None, compensated=True, h_sum="ff", rows=32,
+         h_mode="auto", H_gpu=None, compensated=True, h_sum="ff", ctas=2048,
          repeats=3, verbose=False):
     """Time every (CPL, angles per CTA) candidate for this problem and cache
     the fastest.  Returns {"cols_per_lane", "angles_per_cta", "ms",
@@ -86,20 +88,28 @@ def tune(seg_list, s_dev_arr, grid, xtal, *, precision="fp32",
     from .laue import _solve
     torch = _lib.torch_cuda()
     prec = as_precision(precision)
-    small = grid.replace(beam_width=rows * grid.dx) if H_gpu is None else grid
     s = np.atleast_1d(np.asarray(s_dev_arr, float))
-    geo = grid_arrays(small)
+    full = grid_arrays(grid)
+    full_rows = int(np.sum(np.abs((np.arange(full["Ny"]) - full["Ny"] // 2)
+                                  * full["dx"]) < full["fov_hy"]))
     results = []
     ev0, ev1 = torch.cuda.Event(enable_timing=True), \
         torch.cuda.Event(enable_timing=True)
-    out = torch.empty((len(s), geo["Ny"], geo["Nx"]), dtype=prec.torch_complex,
-                      device="cuda")
     for cpl in CPL[prec.name]:
-        if -(-geo["Nx"] // (32 * cpl)) > 32:
+        if -(-full["Nx"] // (32 * cpl)) > 32:
             continue
         for A in ANGLES:
             if A > len(s):
                 continue
+            groups = -(-len(s) // A)
+            rows = min(full_rows, max(32, -(-ctas // groups)))
+            small = grid if (H_gpu is not None or rows >= full_rows) else \
+                grid.replace(beam_width=rows * grid.dx)
+            geo = grid_arrays(small)
+            n_rows = int(np.sum(np.abs((np.arange(geo["Ny"]) - geo["Ny"] // 2)
+                                       * geo["dx"]) < geo["fov_hy"]))
+            out = torch.empty((len(s), geo["Ny"], geo["Nx"]),
+                              dtype=prec.torch_complex, device="cuda")
             try:
                 kw = dict(h_mode=h_mode, angles_per_cta=A, cols_per_lane=cpl,
                           out=out, tuned=False, compensated=compensated,
@@ -116,9 +126,10 @@ def tune(seg_list, s_dev_arr, grid, xtal, *, precision="fp32",
                     best = min(best, ev0.elapsed_time(ev1))
             except (ValueError, NotImplementedError, MemoryError):
                 continue
-            results.append((cpl, A, best))
+            results.append((cpl, A, best / n_rows * full_rows))
             if verbose:
-                print(f"cpl {cpl:2d} angles/CTA {A}: {best:.3f} ms")
+                print(f"cpl {cpl:2d} angles/CTA {A}: {best:.3f} ms on "
+                      f"{n_rows} rows, {results[-1][2]:.3f} ms scaled")
     if not results:
         raise RuntimeError("no launch shape could run this problem")
     cpl, A, ms = min(results, key=lambda r: r[2])
@@ -127,7 +138,7 @@ def tune(seg_list, s_dev_arr, grid, xtal, *, precision="fp32",
                  h_mode=h_mode, compensated=compensated, h_sum=h_sum)
     with _lock:
         _load()[signature(d)] = {"cols_per_lane": cpl, "angles_per_cta": A,
-                                 "ms_reduced_rows": ms, "rows": rows}
+                                 "ms_full_estimate": ms}
         _save()
     return {"cols_per_lane": cpl, "angles_per_cta": A, "ms": ms,
             "candidates": results}

@@ -321,6 +321,7 @@ struct FastConfig {
     MarchEntry entry;
     int cpl, WA, A, block;
     size_t smem;
+    int stage = ST_COMPUTE, raw_elem = 0;
 };
 
 static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
@@ -383,10 +384,33 @@ static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
     fc->A = A;
     fc->block = 32 * fc->WA * A;
     MarchSmem sm = single
-        ? march_smem<float>(best, fc->WA, A, d->Nz, p.hsrc, d->n_seg, comp)
-        : march_smem<double>(best, fc->WA, A, d->Nz, p.hsrc, d->n_seg, false);
+        ? march_smem<float>(best, fc->WA, A, d->Nz, p.hsrc, d->n_seg, comp,
+                            fc->stage, fc->raw_elem)
+        : march_smem<double>(best, fc->WA, A, d->Nz, p.hsrc, d->n_seg, false,
+                             fc->stage, fc->raw_elem);
     fc->smem = sm.total;
     return DYFOX_OK;
+}
+
+// Staging mode of a grid source: rows are copied with 16-byte cp.async, so
+// the base must be 16-byte aligned and a row a multiple of 16 bytes.
+static void choose_stage(const dyfox_laue_desc *d, const LauePlan &p,
+                         const void *base, FastConfig *fc) {
+    const bool single = d->precision == DYFOX_FP32;
+    fc->stage = ST_COMPUTE;
+    fc->raw_elem = 0;
+    int elem = 0;
+    switch (p.hsrc) {
+    case HS_GRID64: elem = 8; break;
+    case HS_GRID32: elem = 4; break;
+    case HS_CS32: elem = 8; break;
+    case HS_CS64: elem = 16; break;
+    default: return;
+    }
+    if (((uintptr_t)base & 15) || ((size_t)d->Nx * elem) % 16) return;
+    fc->raw_elem = elem;
+    fc->stage = ((p.hsrc == HS_CS32 && single) || (p.hsrc == HS_CS64 && !single))
+                    ? ST_DIRECT : ST_CONVERT;
 }
 
 static int smem_limit(size_t need) {
@@ -534,12 +558,15 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     }
 
     FastConfig fc;
+    choose_stage(d, p, p.stage ? (const void *)a.csgrid : h_grid, &fc);
     if ((st = choose_fast(d, p, &fc))) return st;
     if ((st = smem_limit(fc.smem))) return st;
     a.WA = fc.WA;
     a.A = fc.A;
     a.ncols = 32 * fc.WA * fc.cpl;
     a.n_groups = div_up(d->n_e, fc.A);
+    a.stage = fc.stage;
+    a.raw_elem = fc.raw_elem;
     e = fc.entry.launch(a, p.n_rows * a.n_groups, fc.block, fc.smem, stream);
     if (e) return cuda_status(e, "laue_march");
     return DYFOX_OK;

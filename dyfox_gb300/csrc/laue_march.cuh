@@ -69,6 +69,8 @@ struct MarchArgs {
     const float4 *kappa32;      // the same, rounded to float (FP32 march)
     const double2 *scale;       // (n_e): M22^(Nz-1)
     void *out;                  // (n_e, Ny, Nx) complex (R2)
+    int stage;                  // StageMode of a GENERIC source
+    int raw_elem;               // bytes per column of a staged raw row
 };
 
 // Input beam D0(z=0) at column x (kernels.py:77-88), in double.
@@ -149,21 +151,41 @@ __device__ __forceinline__ float fmaR(float a, float b, float c) {
     return fmaf(a, b, c);
 }
 
+// How the e^{iH} row of each depth step reaches shared memory.
+//   ST_COMPUTE  the producer evaluates every column (Volterra field,
+//               closed form, perfect crystal, or a grid that cannot be
+//               staged asynchronously);
+//   ST_DIRECT   staged e^{iH} rows of the march's own precision are copied
+//               with cp.async two steps ahead into three stages and read in
+//               place by the update;
+//   ST_CONVERT  raw rows (H grids, or e^{iH} of the other precision) are
+//               copied the same way and turned into e^{iH} by the producer.
+enum StageMode { ST_COMPUTE = 0, ST_DIRECT = 1, ST_CONVERT = 2 };
+
 // Shared-memory plan of the march kernel (bytes), shared with the host.
+// Rows use the natural column layout: element x of a row is column x; lane
+// L reads x = L * CPL + j (odd CPL keeps 8-byte reads conflict-free).
 struct MarchSmem {
-    size_t cs, bnd, an, segf, piv, hc, total;
+    size_t cs, raw, raw_stage, bnd, an, segf, hc, total;
 };
 
 template <typename R>
 __host__ __device__ inline MarchSmem march_smem(int CPL, int WA, int A,
                                                 int Nz, int hsrc, int n_seg,
-                                                bool comp) {
+                                                bool comp, int stage,
+                                                int raw_elem) {
     using R2 = typename RT<R>::R2;
     MarchSmem m;
-    int PS = 32 * WA + 1;
-    int nwarps = WA * A;
-    m.cs = 0;
-    size_t off = (size_t)2 * CPL * PS * sizeof(R2);
+    const size_t ncols = (size_t)32 * WA * CPL;
+    const int nwarps = WA * A;
+    size_t off = 0;
+    m.cs = off;
+    if (stage != ST_DIRECT) off += 2 * ncols * sizeof(R2);
+    off = (off + 15) & ~(size_t)15;
+    m.raw = off;
+    m.raw_stage = stage != ST_COMPUTE
+        ? ((ncols * raw_elem + 15) & ~(size_t)15) : 0;
+    off += 3 * m.raw_stage;
     m.bnd = off;
     off += (size_t)2 * nwarps * (comp ? 4 : 2) * sizeof(R2);
     off = (off + 15) & ~(size_t)15;
@@ -173,11 +195,24 @@ __host__ __device__ inline MarchSmem march_smem(int CPL, int WA, int A,
     m.segf = off;
     if (hsrc == HS_SEG && sizeof(R) == 4) off += (size_t)n_seg * sizeof(SegF);
     off = (off + 15) & ~(size_t)15;
-    m.piv = off;
     m.hc = off;
     off += sizeof(double);
     m.total = off;
     return m;
+}
+
+__device__ __forceinline__ void cp_async16(void *dst_smem, const void *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 template <typename R, int CPL, int HT, bool COMP>
@@ -185,7 +220,6 @@ __global__ void laue_march_kernel(const MarchArgs a) {
     using R2 = typename RT<R>::R2;
     extern __shared__ __align__(16) unsigned char smem[];
     const int WA = a.WA;
-    const int PS = 32 * WA + 1;
     const int nthreads = blockDim.x;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nwarps = nthreads >> 5;
@@ -196,11 +230,13 @@ __global__ void laue_march_kernel(const MarchArgs a) {
     const int iy = a.row0 + row_blk;
     const int ie_raw = grp * a.A + g;
     const int ie = ie_raw < a.n_e ? ie_raw : a.n_e - 1;
-    const int Nx = a.Nx, Nz = a.Nz, nsteps = Nz - 1;
+    const int Nx = a.Nx, Nz = a.Nz, nsteps = Nz - 1, ncols = a.ncols;
     const int hsrc = HT != HT_GENERIC ? HS_SEG : a.hsrc;
+    const int stage = HT != HT_GENERIC ? (int)ST_COMPUTE : a.stage;
     const MarchSmem plan = march_smem<R>(CPL, WA, a.A, Nz, hsrc, a.n_seg,
-                                         COMP);
+                                         COMP, stage, a.raw_elem);
     R2 *cs = reinterpret_cast<R2 *>(smem + plan.cs);
+    unsigned char *raw = smem + plan.raw;
     R2 *bnd = reinterpret_cast<R2 *>(smem + plan.bnd);
     R2 *an_cs = reinterpret_cast<R2 *>(smem + plan.an);
     SegF *segf = reinterpret_cast<SegF *>(smem + plan.segf);
@@ -219,7 +255,15 @@ __global__ void laue_march_kernel(const MarchArgs a) {
         for (int k = tid; k < nsteps; k += nthreads)
             an_cs[k] = CS<R>::of_f64(analytic_h(a.an, y_pix, k, a.dz));
     }
-    if ((HT != HT_GENERIC && kSingle) || hsrc == HS_ANALYTIC) __syncthreads();
+    if (stage == ST_DIRECT) {
+        // Columns beyond Nx of every stage read as zero coupling.
+        for (int st = 0; st < 3; ++st) {
+            R2 *row = reinterpret_cast<R2 *>(raw + (size_t)st * plan.raw_stage);
+            for (int x = Nx + tid; x < ncols; x += nthreads)
+                row[x] = R2{R(0), R(0)};
+        }
+    }
+    __syncthreads();
     // Sum over segments of the constant the single evaluator drops (double),
     // and that sum reduced mod 2 pi (start of the float-float sum).
     double hconst = 0.0;
@@ -229,13 +273,35 @@ __global__ void laue_march_kernel(const MarchArgs a) {
         hcr = reduce_2pi(hconst);
     }
 
-    // Produces e^{iH(kk, x)} of every padded column into buffer `buf`.
+    // Asynchronous copy of the raw row of step kk into stage kk % 3; every
+    // thread commits one group per call, copy or not.
+    const unsigned char *raw_src = nullptr;
+    size_t raw_row = 0;
+    if (stage != ST_COMPUTE) {
+        const bool grid = hsrc == HS_GRID64 || hsrc == HS_GRID32;
+        raw_src = static_cast<const unsigned char *>(grid ? a.hgrid : a.csgrid);
+        raw_row = grid ? (size_t)iy * Nz : (size_t)row_blk * nsteps;
+    }
+    const int chunks = (Nx * a.raw_elem) >> 4;
+    auto stage_issue = [&](int kk) {
+        if (kk < nsteps) {
+            const unsigned char *src =
+                raw_src + (raw_row + kk) * (size_t)Nx * a.raw_elem;
+            unsigned char *dst = raw + (size_t)(kk % 3) * plan.raw_stage;
+            for (int c = tid; c < chunks; c += nthreads)
+                cp_async16(dst + 16 * c, src + 16 * c);
+        }
+        cp_async_commit();
+    };
+
+    // e^{iH(kk, x)} of every padded column into cs buffer `buf`.
     auto produce = [&](int kk, int buf) {
-        R2 *dst = cs + (size_t)buf * CPL * PS;
+        R2 *dst = cs + (size_t)buf * ncols;
+        const unsigned char *st = raw + (size_t)(kk % 3) * plan.raw_stage;
 #pragma unroll
         for (int i = 0; i < CPL; ++i) {
             const int x = tid + i * nthreads;
-            if (x >= a.ncols) continue;
+            if (x >= ncols) continue;
             R2 v;
             if (x >= Nx) {
                 v.x = R(0); v.y = R(0);
@@ -275,6 +341,20 @@ __global__ void laue_march_kernel(const MarchArgs a) {
                     }
                     v = CS<R>::of_f64(acc);
                 }
+            } else if (stage == ST_CONVERT) {
+                switch (hsrc) {
+                case HS_GRID64:
+                    v = CS<R>::of_f64(reinterpret_cast<const double *>(st)[x]);
+                    break;
+                case HS_GRID32:
+                    v = CS<R>::of_f32(reinterpret_cast<const float *>(st)[x]);
+                    break;
+                case HS_CS32:
+                    v = CS<R>::of_cs(reinterpret_cast<const float2 *>(st)[x]);
+                    break;
+                default:
+                    v = CS<R>::of_cs(reinterpret_cast<const double2 *>(st)[x]);
+                }
             } else {
                 switch (hsrc) {
                 case HS_GRID64:
@@ -304,7 +384,7 @@ __global__ void laue_march_kernel(const MarchArgs a) {
                     v.x = R(1); v.y = R(0);
                 }
             }
-            dst[(x % CPL) * PS + x / CPL] = v;
+            dst[x] = v;
         }
     };
 
@@ -319,7 +399,19 @@ __global__ void laue_march_kernel(const MarchArgs a) {
         Ai[j] = R(0); Br[j] = R(0); Bi[j] = R(0);
         if constexpr (COMP) { Alr[j] = 0; Ali[j] = 0; Blr[j] = 0; Bli[j] = 0; }
     }
-    produce(0, 0);
+    if (stage == ST_DIRECT) {
+        stage_issue(0);
+        stage_issue(1);
+        cp_async_wait<1>();
+    } else if (stage == ST_CONVERT) {
+        stage_issue(0);
+        stage_issue(1);
+        cp_async_wait<0>();
+        __syncthreads();
+        produce(0, 0);
+    } else {
+        produce(0, 0);
+    }
     if (lane == 0) {
         bnd[(0 * nwarps + warp) * NB + 0] = R2{Ar[0], Ai[0]};
         if constexpr (COMP) bnd[(0 * nwarps + warp) * NB + 2] = R2{Alr[0], Ali[0]};
@@ -348,7 +440,8 @@ __global__ void laue_march_kernel(const MarchArgs a) {
             k21r = (R)kn.k21.x; k21i = (R)kn.k21.y;
             if (k + 1 < nsteps) kn = ldg_kappa(kap + k + 1);
         }
-        if (k + 1 < nsteps) produce(k + 1, p ^ 1);
+        if (stage != ST_COMPUTE) stage_issue(k + 2);
+        if (stage != ST_DIRECT && k + 1 < nsteps) produce(k + 1, p ^ 1);
 
         // Neighbour values of the previous state.
         R ainr = __shfl_down_sync(0xffffffffu, Ar[0], 1);
@@ -386,7 +479,10 @@ __global__ void laue_march_kernel(const MarchArgs a) {
                 binr = 0; bini = 0; binlr = 0; binli = 0;
             }
         }
-        const R2 *src = cs + (size_t)p * CPL * PS + L;
+        const R2 *src = (stage == ST_DIRECT
+                             ? reinterpret_cast<const R2 *>(
+                                   raw + (size_t)(k % 3) * plan.raw_stage)
+                             : cs + (size_t)p * ncols) + L * CPL;
         R pbr = binr, pbi = bini, pblr = binlr, pbli = binli;
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
@@ -394,7 +490,7 @@ __global__ void laue_march_kernel(const MarchArgs a) {
             const R ai = j + 1 < CPL ? Ai[j + 1] : aini;
             const R br = pbr, bi = pbi;
             pbr = Br[j]; pbi = Bi[j];
-            const R2 e = src[j * PS];
+            const R2 e = src[j];
             const R m12r = k12r * e.x - k12i * e.y;
             const R m12i = k12r * e.y + k12i * e.x;
             const R m21r = k21r * e.x + k21i * e.y;
@@ -430,8 +526,13 @@ __global__ void laue_march_kernel(const MarchArgs a) {
             if constexpr (COMP)
                 bnd[(q * nwarps + warp) * NB + 3] = R2{Blr[CPL - 1], Bli[CPL - 1]};
         }
+        // The stage of step k + 1 (DIRECT) or k + 2 (CONVERT) is complete
+        // and, after the barrier, visible to every thread.
+        if (stage == ST_DIRECT) cp_async_wait<1>();
+        else if (stage == ST_CONVERT) cp_async_wait<0>();
         __syncthreads();
     }
+    if (stage != ST_COMPUTE) cp_async_wait<0>();
 
     // ---------------------------------------------------------- output
     if (ie_raw >= a.n_e) return;

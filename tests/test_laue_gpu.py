@@ -388,7 +388,7 @@ def test_autotuner_caches_a_shape_that_changes_nothing(gpu, diamond400,
     before = np_(solve_dislocation(seg, s, small_grid, diamond400,
                                    precision="fp32"))
     r = autotune.tune(seg, s, small_grid, diamond400, precision="fp32",
-                      rows=8)
+                      ctas=64)
     assert len(r["candidates"]) >= 2
     assert (tmp_path / "tune.json").exists()
     d = describe(seg, s, small_grid, diamond400, precision="fp32")
