@@ -44,6 +44,10 @@ WORKLOAD = ("laue-readme: diamond(400) 17 keV, t=200um dx=0.25um "
             "beam_width=120um (Ny x Nx = 544 x 800, Nz=359), 1 edge "
             "dislocation line [101] b=(a/2)[10-1] at depth t/2, "
             "s_dev at 0 and 117.5 urad")
+# DRAM bytes (read + write) of one launch of the chosen-form march on the
+# readme workload, from the ncu capture summarised in
+# profiles/laue_march_fp32_readme.md.
+MARCH_FP32_README_DRAM_BYTES = 2832896
 
 
 def parse():
@@ -342,14 +346,19 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(host.numel() * 8)},
         "roofline": {"bound": "fp32", "achieved": achieved,
                      "peak": peaks["fp32"], "unit": "TFLOP/s",
-                     "frac": achieved / peaks["fp32"], "traffic": None,
+                     "frac": achieved / peaks["fp32"],
+                     "traffic": MARCH_FP32_README_DRAM_BYTES,
+                     "traffic_source": "ncu dram__bytes_read.sum + "
+                                       "dram__bytes_write.sum of one launch "
+                                       "(profiles/laue_march_fp32_readme.md)",
                      "peak_source": "measured FFMA throughput "
                                     "(dyfox_pipe_peak, this run)",
                      "algorithmic_flops_per_launch": flops},
         "pipe_peaks_tflops": peaks,
         "launch_shape": {"tuned": tuned or None,
                          "autotuner": "dyfox_gb300.autotune (cols per lane x "
-                                      "angles per CTA, timed on 32 rows)"},
+                                      "angles per CTA, each timed at about "
+                                      "2048 CTAs)"},
         "gpu_launches": int(launches),
         "wall_s": wall,
     }
