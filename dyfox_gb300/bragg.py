@@ -17,11 +17,19 @@ larger (up to ``restart_cap``), at most ``tries`` times.
 
 ``solve_scan`` is the batched form: many deviation parameters over the same
 planes in one launch.
+
+``precision=FP32`` (keyword-only) selects the mixed-precision solve: the
+Krylov products (march and preconditioner) run in single precision, while
+the right-hand side, every true residual, the orthogonalisation, the
+rotations and the solution stay in double, each restart being one step of
+iterative refinement.  It stops on the same true relative residual
+``tol`` as the FP64 solve, so its answers agree with FP64 to about ``tol``.
 """
 
 import numpy as np
 
 from . import _lib
+from .backend import FP64, precision as as_precision
 from .bragg_geometry import (BraggConfig, bragg_g_vector,  # noqa: F401
                              edge_segment, threading_segment)
 
@@ -65,7 +73,7 @@ def _L():
     return L
 
 
-def _desc(cfg, xtal, n_y, n_s, n_seg, tol, restart, maxiter):
+def _desc(cfg, xtal, n_y, n_s, n_seg, tol, restart, maxiter, prec=FP64):
     d = BraggDesc()
     for name in ("sig0", "sig_h", "sig_hbar"):
         v = complex(getattr(xtal, name))
@@ -80,15 +88,17 @@ def _desc(cfg, xtal, n_y, n_s, n_seg, tol, restart, maxiter):
     d.beam_thickness = 0.0 if bt is None else float(bt)
     d.beam_centre = float(getattr(cfg, "beam_centre", 0.0))
     d.tol, d.restart, d.maxiter = float(tol), int(restart), int(maxiter)
-    d.precision = _lib.DYFOX_FP64
+    d.precision = as_precision(prec).code
     return d
 
 
 class _Problem:
     """Device-side inputs of one call: segment table, planes, s values."""
 
-    def __init__(self, seg_list, s_values, cfg, y_values, xtal, g_vec):
+    def __init__(self, seg_list, s_values, cfg, y_values, xtal, g_vec,
+                 precision=FP64):
         torch = _lib.torch_cuda()
+        self.prec = as_precision(precision)
         self.torch = torch
         self.cfg, self.xtal = cfg, xtal
         self.seg_list, self.g_vec = seg_list or [], g_vec
@@ -106,7 +116,7 @@ class _Problem:
     def desc(self, tol=1e-10, restart=40, maxiter=25, n_s=None):
         return _desc(self.cfg, self.xtal, len(self.y),
                      len(self.s) if n_s is None else n_s, self.n_seg, tol,
-                     restart, maxiter)
+                     restart, maxiter, self.prec)
 
     def workspace(self, d):
         n = _L().dyfox_bragg_workspace_bytes(d)
@@ -120,14 +130,15 @@ def _yp(prob):
 
 
 def solve_scan(seg_list, s_values, cfg, y_values, xtal, g_vec, tol=1e-10,
-               restart=40, maxiter=25, x0=None):
+               restart=40, maxiter=25, x0=None, *, precision=FP64):
     """All deviation parameters x all planes in one launch.
 
     Returns (out, info): out is a (n_s, n_y, Nx) complex128 CUDA tensor of
     physical exit waves; info a (n_s * n_y, 4) CUDA tensor of (true relative
     residual, inner iterations, code, |b|) per system.
     """
-    prob = _Problem(seg_list, s_values, cfg, y_values, xtal, g_vec)
+    prob = _Problem(seg_list, s_values, cfg, y_values, xtal, g_vec,
+                    precision)
     return _run(prob, tol, restart, maxiter, x0)
 
 
@@ -149,7 +160,7 @@ def solve_surface_batch(seg_list, s_dev, cfg, y_values, xtal, g_vec,
                         xp=None, chunk=32, tol=1e-10, restart=40, maxiter=25,
                         verbose=False, gpu_gmres=True, accept=1e-7, grow=4,
                         tries=3, restart_cap=256, max_depth=6, per_plane=6,
-                        chunk_cap=32):
+                        chunk_cap=32, *, precision=FP64):
     """Exit wave on the (ny, Nx) surface grid for one deviation parameter.
 
     Returns (NumPy complex128 (ny, Nx), info) with info keys ``residual``
@@ -158,7 +169,8 @@ def solve_surface_batch(seg_list, s_dev, cfg, y_values, xtal, g_vec,
     ``unconverged_chunks`` (planes above ``accept``) and ``converged``.
     """
     torch = _lib.torch_cuda()
-    prob = _Problem(seg_list, [float(s_dev)], cfg, y_values, xtal, g_vec)
+    prob = _Problem(seg_list, [float(s_dev)], cfg, y_values, xtal, g_vec,
+                    precision)
     out, info = _run(prob, tol, restart, maxiter)
     res = info[:, 0].cpu().numpy()
     its = int(info[:, 1].max().item()) if len(res) else 0
@@ -170,7 +182,7 @@ def solve_surface_batch(seg_list, s_dev, cfg, y_values, xtal, g_vec,
         r = min(r * grow, restart_cap)
         retries += 1
         sub = _Problem(seg_list, [float(s_dev)], cfg, prob.y[bad], xtal,
-                       g_vec)
+                       g_vec, precision)
         # warm start from the previous solution (undo the phase restoration)
         e0h = torch.exp(-1j * _plane_H0(sub))
         x0 = (out[0, torch.as_tensor(bad, device="cuda")] / e0h)[None]
@@ -199,10 +211,12 @@ def _plane_H0(prob):
 
 
 def solve_bragg_stable(seg_list, s_dev, cfg, xtal, g_vec, xp=None,
-                       tol=1e-10, y_plane=0.0, restart=40, maxiter=20):
+                       tol=1e-10, y_plane=0.0, restart=40, maxiter=20, *,
+                       precision=FP64):
     """One plane: (exit wave, {gmres_code, iterations, residual}).  The wave
     is a NumPy array when ``xp`` is None or NumPy, else a CUDA tensor."""
-    prob = _Problem(seg_list, [float(s_dev)], cfg, [y_plane], xtal, g_vec)
+    prob = _Problem(seg_list, [float(s_dev)], cfg, [y_plane], xtal, g_vec,
+                    precision)
     out, info = _run(prob, tol, restart, maxiter)
     inf = info[0].cpu().numpy()
     wave = out[0, 0]
@@ -213,11 +227,13 @@ def solve_bragg_stable(seg_list, s_dev, cfg, xtal, g_vec, xp=None,
 
 
 def apply_operator(seg_list, s_values, cfg, y_values, xtal, g_vec, mode,
-                   in0=None, in1=None):
+                   in0=None, in1=None, *, precision=FP64):
     """The down-march (mode "march": D_g(t) of (D0(0), Dg(0)) = (in0, in1))
     or the preconditioner (mode "precond": M in0) for every (s, plane);
-    inputs and output are (n_s, n_y, Nx) complex128 CUDA tensors."""
-    prob = _Problem(seg_list, s_values, cfg, y_values, xtal, g_vec)
+    inputs and output are (n_s, n_y, Nx) complex128 CUDA tensors.
+    precision=FP32: the single-precision operators of the mixed solve."""
+    prob = _Problem(seg_list, s_values, cfg, y_values, xtal, g_vec,
+                    precision)
     torch = prob.torch
     d = prob.desc()
     ws = prob.workspace(d)

@@ -10,6 +10,16 @@
 // Gram-Schmidt Arnoldi, Givens rotations (LAPACK lartg), adaptive inner
 // tolerance, true residual at every restart).  The exit wave is
 // v e^{-iH(z=0)}.
+//
+// Precision DYFOX_FP32 is a mixed-precision form of the same solve: the
+// Arnoldi products (march and preconditioner) run in single precision
+// while b, every true residual, the Gram-Schmidt coefficients, the Givens
+// rotations and the solution stay in double.  Each restart is then one step
+// of iterative refinement on the double residual, so the solve still stops
+// at true relative residual <= tol computed in double; a restart cycle
+// stops its inner iteration once the estimated residual has dropped by
+// kMixedInnerDrop, below which the single-precision operator's own error
+// makes further inner steps useless.
 #include <math.h>
 #include <string.h>
 
@@ -27,6 +37,8 @@ struct BraggArgs {
     const double2 *inc;           // (Nx): incident D0
     const double2 *iT;            // (n_s, Nx): 1 / T22s
     const double2 *tw;            // (Nx): exp(-2 pi i m / Nx)
+    const float2 *cb32, *ch32;    // FP32 copies of cb, ch (mixed form)
+    const float2 *iT32, *tw32;    // FP32 copies of iT, tw (mixed form)
     FftPlan plan;
     double2 *V;                   // (n_sys, m + 1, Nx)
     double2 *Hh;                  // (n_sys, m, m + 1)
@@ -52,13 +64,15 @@ __device__ __forceinline__ void step_factors(const BraggArgs &a, int is,
 // Couplings of every plane: cb = ds (sigma_hbar e^{+iH}), ch = ds (sigma_h
 // e^{-iH}) with H the Volterra phase at (x_i, y_p, z_k) summed in segment
 // order; e0h = e^{-iH} at k = 0.  One thread per voxel.
+// cb32, ch32 (may be NULL): the same couplings rounded to float.
 __global__ void bragg_couple_kernel(const double *__restrict__ segs,
                                     int n_seg, int Nx, int Nz, double dx,
                                     double dz, VolterraConsts vc,
                                     const double *__restrict__ y, int n_y,
                                     double ds, double shr, double shi,
                                     double sbr, double sbi, double2 *cb,
-                                    double2 *ch, double2 *e0h) {
+                                    double2 *ch, double2 *e0h, float2 *cb32,
+                                    float2 *ch32) {
     const long total = (long)n_y * Nz * Nx;
     for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total;
          idx += (long)gridDim.x * blockDim.x) {
@@ -80,29 +94,37 @@ __global__ void bragg_couple_kernel(const double *__restrict__ segs,
         // sigma e^{-+iH}, then ds times each part (solver.py:260-261, 31-32)
         const double2 a = make_double2(shr * c + shi * sn, shi * c - shr * sn);
         const double2 b = make_double2(sbr * c - sbi * sn, sbi * c + sbr * sn);
-        cb[idx] = make_double2(ds * b.x, ds * b.y);
-        ch[idx] = make_double2(ds * a.x, ds * a.y);
+        const double2 vb = make_double2(ds * b.x, ds * b.y);
+        const double2 vh = make_double2(ds * a.x, ds * a.y);
+        cb[idx] = vb;
+        ch[idx] = vh;
+        if (cb32) {
+            cb32[idx] = make_float2((float)vb.x, (float)vb.y);
+            ch32[idx] = make_float2((float)vh.x, (float)vh.y);
+        }
         if (k == 0) e0h[(size_t)p * Nx + x] = make_double2(c, -sn);
     }
 }
 
-// exp(-2 pi i m / N) for m in [0, N).
-__global__ void twiddle_kernel(double2 *tw, int N) {
+// exp(-2 pi i m / N) for m in [0, N); tw32 (may be NULL) rounded to float.
+__global__ void twiddle_kernel(double2 *tw, float2 *tw32, int N) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= N) return;
     double sn, c;
     sincospi(-2.0 * m / N, &sn, &c);
     tw[m] = make_double2(c, sn);
+    if (tw32) tw32[m] = make_float2((float)c, (float)sn);
 }
 
 // perfect_symbol (bragg/solver.py:38-60): per Fourier mode the 2 x 2 chain
 // of the unstrained down-march; T22 floored at 1e-8 max|T22| (164-165,
-// 277-278) and inverted into iT.  One CTA per deviation parameter.
+// 277-278) and inverted into iT (and into iT32, rounded to float, when
+// not NULL).  One CTA per deviation parameter.
 __global__ void bragg_symbol_kernel(const double *__restrict__ s_dev, int Nx,
                                     int Nz, double ds, double s0r, double s0i,
                                     double shr, double shi, double sbr,
                                     double sbi, double2 *T21, double2 *T22,
-                                    double2 *iT) {
+                                    double2 *iT, float2 *iT32) {
     __shared__ double2 red[33];
     const int is = blockIdx.x;
     const double alpha = -2.0 * kPi * s_dev[is];
@@ -146,7 +168,10 @@ __global__ void bragg_symbol_kernel(const double *__restrict__ s_dev, int Nx,
         double2 t = iT[(size_t)is * Nx + x];
         if (hypot(t.x, t.y) < floor_) t = make_double2(floor_, 0.0);
         const double d = t.x * t.x + t.y * t.y;
-        iT[(size_t)is * Nx + x] = make_double2(t.x / d, -t.y / d);
+        const double2 v = make_double2(t.x / d, -t.y / d);
+        iT[(size_t)is * Nx + x] = v;
+        if (iT32)
+            iT32[(size_t)is * Nx + x] = make_float2((float)v.x, (float)v.y);
     }
 }
 
@@ -175,7 +200,11 @@ __device__ void lartg(double2 f, double2 g, double &c, double2 &s,
     }
 }
 
-template <int CPL>
+// Drop of the estimated (preconditioned) residual after which a restart
+// cycle of the mixed form ends its inner iteration.
+constexpr double kMixedInnerDrop = 1e-5;
+
+template <int CPL, bool MIXED>
 __global__ void bragg_gmres_kernel(const BraggArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int Nx = a.Nx, m = a.restart;
@@ -200,6 +229,11 @@ __global__ void bragg_gmres_kernel(const BraggArgs a) {
     double2 *B = a.B + (size_t)sys * Nx;
     double2 e0, ieg;
     step_factors(a, is, e0, ieg);
+    const float2 e0f = make_float2((float)e0.x, (float)e0.y);
+    const float2 iegf = make_float2((float)ieg.x, (float)ieg.y);
+    const float2 *cb32 = MIXED ? a.cb32 + (size_t)iy * a.Nz * Nx : nullptr;
+    const float2 *ch32 = MIXED ? a.ch32 + (size_t)iy * a.Nz * Nx : nullptr;
+    const float2 *iT32 = MIXED ? a.iT32 + (size_t)is * Nx : nullptr;
     const double eps = 2.220446049250313e-16;
 
     auto norm2 = [&](const double2 *v) {
@@ -213,6 +247,24 @@ __global__ void bragg_gmres_kernel(const BraggArgs a) {
                                   A0, A1, W);
         else bragg_march<CPL>(cb, ch, e0, ieg, a.Nz, Nx, a.inc, nullptr, A0,
                               A1, W);
+    };
+    // The Arnoldi operator: W <- M A src, in single precision when MIXED.
+    auto inner_op = [&](const double2 *src) {
+        if (MIXED) {
+            bragg_march32<CPL>(cb32, ch32, e0f, iegf, a.Nz, Nx, nullptr, src,
+                               reinterpret_cast<float2 *>(A0),
+                               reinterpret_cast<float2 *>(A1), W);
+        } else {
+            matvec(src);
+        }
+    };
+    auto precond = [&]() {
+        if (MIXED)
+            precond_apply32(W, reinterpret_cast<float2 *>(A0),
+                            reinterpret_cast<float2 *>(A1), a.plan, a.tw32,
+                            iT32);
+        else
+            precond_apply(W, A0, A1, a.plan, a.tw, iT);
     };
 
     // b = -d
@@ -232,7 +284,7 @@ __global__ void bragg_gmres_kernel(const BraggArgs a) {
         const double atol = a.tol * bnrm2;
         for (int x = tid; x < Nx; x += nt) W[x] = B[x];
         __syncthreads();
-        precond_apply(W, A0, A1, a.plan, a.tw, iT);
+        precond();
         const double Mb_nrm2 = norm2(W);
         double ptol_max_factor = 1.0;
         double ptol = Mb_nrm2 * fmin(ptol_max_factor, atol / bnrm2);
@@ -258,8 +310,11 @@ __global__ void bragg_gmres_kernel(const BraggArgs a) {
         } else {
             for (int iter = 0; iter < a.maxiter; ++iter) {
                 // v0 = M r / |M r|, S = (|M r|, 0, ...)
-                precond_apply(W, A0, A1, a.plan, a.tw, iT);
+                precond();
                 const double tmp = norm2(W);
+                // inner stopping level of this cycle
+                const double pstop =
+                    MIXED ? fmax(ptol, kMixedInnerDrop * tmp) : ptol;
                 for (int x = tid; x < Nx; x += nt) V[x] = cscale(1.0 / tmp, W[x]);
                 for (int j = tid; j <= m; j += nt)
                     S[j] = make_double2(j == 0 ? tmp : 0.0, 0.0);
@@ -267,8 +322,8 @@ __global__ void bragg_gmres_kernel(const BraggArgs a) {
                 bool breakdown = false;
                 int col = 0;
                 for (col = 0; col < m; ++col) {
-                    matvec(V + (size_t)col * Nx);
-                    precond_apply(W, A0, A1, a.plan, a.tw, iT);
+                    inner_op(V + (size_t)col * Nx);
+                    precond();
                     const double h0 = norm2(W);
                     // Modified Gram-Schmidt, one pass per basis vector:
                     // subtract the previous projection, accumulate the next.
@@ -331,7 +386,7 @@ __global__ void bragg_gmres_kernel(const BraggArgs a) {
                     presid = red[33].x;
                     ++inner;
                     __syncthreads();
-                    if (presid <= ptol || breakdown) break;
+                    if (presid <= pstop || breakdown) break;
                 }
                 if (col == m) col = m - 1;
                 // y = R^{-1} S (back substitution; R[row][c] = Hh[c][row])
@@ -394,8 +449,9 @@ __global__ void bragg_gmres_kernel(const BraggArgs a) {
 }
 
 // Matvec / preconditioner for parity checks: one CTA per system.
-// mode 0: out = march(d0, dg); mode 1: out = M in.
-template <int CPL>
+// mode 0: out = march(d0, dg); mode 1: out = M in.  MIXED: the
+// single-precision operators of the mixed form.
+template <int CPL, bool MIXED>
 __global__ void bragg_apply_kernel(const BraggArgs a, int mode,
                                    const double2 *d0, const double2 *dg,
                                    double2 *out) {
@@ -409,14 +465,29 @@ __global__ void bragg_apply_kernel(const BraggArgs a, int mode,
     if (mode == 0) {
         double2 e0, ieg;
         step_factors(a, is, e0, ieg);
-        bragg_march<CPL>(a.cb + (size_t)iy * a.Nz * Nx,
-                         a.ch + (size_t)iy * a.Nz * Nx, e0, ieg, a.Nz, Nx,
-                         d0 ? d0 + off : nullptr, dg ? dg + off : nullptr, A0,
-                         A1, W);
+        if (MIXED)
+            bragg_march32<CPL>(a.cb32 + (size_t)iy * a.Nz * Nx,
+                               a.ch32 + (size_t)iy * a.Nz * Nx,
+                               make_float2((float)e0.x, (float)e0.y),
+                               make_float2((float)ieg.x, (float)ieg.y), a.Nz,
+                               Nx, d0 ? d0 + off : nullptr,
+                               dg ? dg + off : nullptr,
+                               reinterpret_cast<float2 *>(A0),
+                               reinterpret_cast<float2 *>(A1), W);
+        else
+            bragg_march<CPL>(a.cb + (size_t)iy * a.Nz * Nx,
+                             a.ch + (size_t)iy * a.Nz * Nx, e0, ieg, a.Nz, Nx,
+                             d0 ? d0 + off : nullptr, dg ? dg + off : nullptr,
+                             A0, A1, W);
     } else {
         for (int x = threadIdx.x; x < Nx; x += blockDim.x) W[x] = d0[off + x];
         __syncthreads();
-        precond_apply(W, A0, A1, a.plan, a.tw, a.iT + (size_t)is * Nx);
+        if (MIXED)
+            precond_apply32(W, reinterpret_cast<float2 *>(A0),
+                            reinterpret_cast<float2 *>(A1), a.plan, a.tw32,
+                            a.iT32 + (size_t)is * Nx);
+        else
+            precond_apply(W, A0, A1, a.plan, a.tw, a.iT + (size_t)is * Nx);
     }
     for (int x = threadIdx.x; x < Nx; x += blockDim.x) out[off + x] = W[x];
 }
@@ -436,7 +507,9 @@ static FftPlan make_fft_plan(int N) {
 
 struct BraggPlan {
     int threads, cpl;
+    bool mixed;
     size_t off_cb, off_ch, off_e0h, off_inc, off_iT, off_tw, off_y;
+    size_t off_cb32, off_ch32, off_iT32, off_tw32;
     size_t off_V, off_H, off_X, off_B, off_info, ws;
 };
 
@@ -459,9 +532,10 @@ static int bragg_validate(const dyfox_bragg_desc *d) {
                   d->ds, d->dx, d->dz, d->tol, d->restart, d->maxiter);
         return DYFOX_EINVAL;
     }
-    if (d->precision != DYFOX_FP64) {
-        set_error("the Bragg solve runs in DYFOX_FP64");
-        return DYFOX_ENOSYS;
+    if (d->precision != DYFOX_FP64 && d->precision != DYFOX_FP32) {
+        set_error("precision %d is neither DYFOX_FP64 nor DYFOX_FP32",
+                  d->precision);
+        return DYFOX_EINVAL;
     }
     return DYFOX_OK;
 }
@@ -486,6 +560,13 @@ static int bragg_plan(const dyfox_bragg_desc *d, BraggPlan *p) {
     p->off_iT = o; o = a256(o + d->n_s * Nx * sizeof(double2));
     p->off_tw = o; o = a256(o + Nx * sizeof(double2));
     p->off_y = o; o = a256(o + d->n_y * sizeof(double));
+    p->mixed = d->precision == DYFOX_FP32;
+    const size_t f32 = p->mixed ? 1 : 0;
+    const size_t plane32 = (size_t)d->Nz * Nx * sizeof(float2) * f32;
+    p->off_cb32 = o; o = a256(o + d->n_y * plane32);
+    p->off_ch32 = o; o = a256(o + d->n_y * plane32);
+    p->off_iT32 = o; o = a256(o + f32 * d->n_s * Nx * sizeof(float2));
+    p->off_tw32 = o; o = a256(o + f32 * Nx * sizeof(float2));
     p->off_V = o; o = a256(o + nsys * (m + 1) * Nx * sizeof(double2));
     p->off_H = o; o = a256(o + nsys * m * (m + 1) * sizeof(double2));
     p->off_X = o; o = a256(o + nsys * Nx * sizeof(double2));
@@ -525,6 +606,12 @@ static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
     a->inc = (double2 *)(ws + p.off_inc);
     a->iT = (double2 *)(ws + p.off_iT);
     a->tw = (double2 *)(ws + p.off_tw);
+    if (p.mixed) {
+        a->cb32 = (const float2 *)(ws + p.off_cb32);
+        a->ch32 = (const float2 *)(ws + p.off_ch32);
+        a->iT32 = (const float2 *)(ws + p.off_iT32);
+        a->tw32 = (const float2 *)(ws + p.off_tw32);
+    }
     a->plan = make_fft_plan(d->Nx);
     a->V = (double2 *)(ws + p.off_V);
     a->Hh = (double2 *)(ws + p.off_H);
@@ -545,23 +632,24 @@ static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
     bragg_couple_kernel<<<(int)blocks, 256, 0, stream>>>(
         seg_table, d->n_seg, d->Nx, d->Nz, d->dx, d->dz,
         volterra_consts(d->nu, d->a_core), y, d->n_y, d->ds, a->shr, a->shi,
-        a->sbr, a->sbi, (double2 *)a->cb, (double2 *)a->ch, (double2 *)a->e0h);
+        a->sbr, a->sbi, (double2 *)a->cb, (double2 *)a->ch, (double2 *)a->e0h,
+        (float2 *)a->cb32, (float2 *)a->ch32);
     incident_kernel<<<div_up(d->Nx, 256), 256, 0, stream>>>(
         (double2 *)a->inc, d->Nx, d->dx, d->beam, d->beam_thickness,
         d->beam_centre);
-    twiddle_kernel<<<div_up(d->Nx, 256), 256, 0, stream>>>((double2 *)a->tw,
-                                                           d->Nx);
+    twiddle_kernel<<<div_up(d->Nx, 256), 256, 0, stream>>>(
+        (double2 *)a->tw, (float2 *)a->tw32, d->Nx);
     bragg_symbol_kernel<<<d->n_s, 256, 0, stream>>>(
         s_dev, d->Nx, d->Nz, d->ds, a->s0r, a->s0i, a->shr, a->shi, a->sbr,
-        a->sbi, nullptr, nullptr, (double2 *)a->iT);
+        a->sbi, nullptr, nullptr, (double2 *)a->iT, (float2 *)a->iT32);
     count_launch(4);
     return cuda_status(cudaGetLastError(), "bragg prepare");
 }
 
-template <int CPL>
+template <int CPL, bool MIXED>
 static cudaError_t launch_gmres(const BraggArgs &a, int threads, size_t smem,
                                 int grid, cudaStream_t stream) {
-    auto *k = bragg_gmres_kernel<CPL>;
+    auto *k = bragg_gmres_kernel<CPL, MIXED>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -572,12 +660,12 @@ static cudaError_t launch_gmres(const BraggArgs &a, int threads, size_t smem,
     return cudaGetLastError();
 }
 
-template <int CPL>
+template <int CPL, bool MIXED>
 static cudaError_t launch_apply(const BraggArgs &a, int threads, size_t smem,
                                 int grid, int mode, const double2 *d0,
                                 const double2 *dg, double2 *out,
                                 cudaStream_t stream) {
-    auto *k = bragg_apply_kernel<CPL>;
+    auto *k = bragg_apply_kernel<CPL, MIXED>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -647,12 +735,22 @@ extern "C" int dyfox_bragg_solve(const dyfox_bragg_desc *d,
     }
     a.out = (double2 *)out;
     const int g = (int)nsys;
-    switch (p.cpl) {
-    case 1: e = launch_gmres<1>(a, p.threads, smem, g, stream); break;
-    case 2: e = launch_gmres<2>(a, p.threads, smem, g, stream); break;
-    case 4: e = launch_gmres<4>(a, p.threads, smem, g, stream); break;
-    case 8: e = launch_gmres<8>(a, p.threads, smem, g, stream); break;
-    default: e = launch_gmres<16>(a, p.threads, smem, g, stream); break;
+    if (p.mixed) {
+        switch (p.cpl) {
+        case 1: e = launch_gmres<1, true>(a, p.threads, smem, g, stream); break;
+        case 2: e = launch_gmres<2, true>(a, p.threads, smem, g, stream); break;
+        case 4: e = launch_gmres<4, true>(a, p.threads, smem, g, stream); break;
+        case 8: e = launch_gmres<8, true>(a, p.threads, smem, g, stream); break;
+        default: e = launch_gmres<16, true>(a, p.threads, smem, g, stream); break;
+        }
+    } else {
+        switch (p.cpl) {
+        case 1: e = launch_gmres<1, false>(a, p.threads, smem, g, stream); break;
+        case 2: e = launch_gmres<2, false>(a, p.threads, smem, g, stream); break;
+        case 4: e = launch_gmres<4, false>(a, p.threads, smem, g, stream); break;
+        case 8: e = launch_gmres<8, false>(a, p.threads, smem, g, stream); break;
+        default: e = launch_gmres<16, false>(a, p.threads, smem, g, stream); break;
+        }
     }
     if (e) return cuda_status(e, "bragg_gmres");
     if (info) {
@@ -697,13 +795,26 @@ extern "C" int dyfox_bragg_apply(const dyfox_bragg_desc *d, int mode,
     cudaError_t e;
     const double2 *i0 = (const double2 *)in0, *i1 = (const double2 *)in1;
     double2 *o = (double2 *)out;
-    switch (p.cpl) {
-    case 1: e = launch_apply<1>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
-    case 2: e = launch_apply<2>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
-    case 4: e = launch_apply<4>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
-    case 8: e = launch_apply<8>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
-    default: e = launch_apply<16>(a, p.threads, smem, nsys, mode, i0, i1, o, stream); break;
+#define DYFOX_APPLY(C, M) \
+    launch_apply<C, M>(a, p.threads, smem, nsys, mode, i0, i1, o, stream)
+    if (p.mixed) {
+        switch (p.cpl) {
+        case 1: e = DYFOX_APPLY(1, true); break;
+        case 2: e = DYFOX_APPLY(2, true); break;
+        case 4: e = DYFOX_APPLY(4, true); break;
+        case 8: e = DYFOX_APPLY(8, true); break;
+        default: e = DYFOX_APPLY(16, true); break;
+        }
+    } else {
+        switch (p.cpl) {
+        case 1: e = DYFOX_APPLY(1, false); break;
+        case 2: e = DYFOX_APPLY(2, false); break;
+        case 4: e = DYFOX_APPLY(4, false); break;
+        case 8: e = DYFOX_APPLY(8, false); break;
+        default: e = DYFOX_APPLY(16, false); break;
+        }
     }
+#undef DYFOX_APPLY
     return cuda_status(e, "bragg_apply");
 }
 
@@ -720,7 +831,7 @@ extern "C" int dyfox_bragg_symbol(const dyfox_bragg_desc *d,
     bragg_symbol_kernel<<<d->n_s, 256, 0, (cudaStream_t)stream_>>>(
         s_dev, d->Nx, d->Nz, d->ds, d->sig0[0], d->sig0[1], d->sig_h[0],
         d->sig_h[1], d->sig_hbar[0], d->sig_hbar[1], (double2 *)T21,
-        (double2 *)T22, nullptr);
+        (double2 *)T22, nullptr, nullptr);
     count_launch(1);
     return cuda_status(cudaGetLastError(), "bragg_symbol");
 }

@@ -1,10 +1,13 @@
 // Building blocks of the Bragg (reflection) shooting solve, one CTA per
-// system (y-plane x deviation parameter), everything in double:
+// system (y-plane x deviation parameter):
 //   * complex helpers and CTA-wide reductions (warp shuffles + one shared
 //     slot per warp, fixed order, so results are deterministic);
-//   * the down-march of DYFOX bragg/solver.py:28-35 (the GMRES matvec);
+//   * the down-march of DYFOX bragg/solver.py:28-35 (the GMRES matvec), in
+//     double and in single precision (the inner products of the mixed
+//     solve);
 //   * a mixed-radix Stockham FFT in shared memory for the perfect-crystal
-//     preconditioner ifft(fft(w) / T22s) of bragg/solver.py:167-168.
+//     preconditioner ifft(fft(w) / T22s) of bragg/solver.py:167-168, in
+//     double and in single precision.
 #pragma once
 #include "common.cuh"
 
@@ -31,6 +34,22 @@ __device__ __forceinline__ double2 cconj(double2 a) {
 }
 __device__ __forceinline__ double cabs2(double2 a) {
     return a.x * a.x + a.y * a.y;
+}
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+    return make_float2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+    return make_float2(a.x - b.x, a.y - b.y);
+}
+__device__ __forceinline__ float2 cmulz(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cconj(float2 a) {
+    return make_float2(a.x, -a.y);
+}
+__device__ __forceinline__ float2 cscale(float s, float2 a) {
+    return make_float2(s * a.x, s * a.y);
 }
 
 // Sum of v over the CTA.  red: shared scratch of >= 33 double2.  Every
@@ -136,6 +155,66 @@ __device__ void bragg_march(const double2 *__restrict__ cb,
     __syncthreads();
 }
 
+// The same march in single precision, for the inner (Arnoldi) products of
+// the mixed-precision solve: couplings cb, ch and the step factors in float,
+// the inputs rounded to float (NULL means zero), the result widened into
+// out.  ex0, ex1: float2 exchange rows of Nx.
+template <int CPL>
+__device__ void bragg_march32(const float2 *__restrict__ cb,
+                              const float2 *__restrict__ ch, float2 e0,
+                              float2 ieg, int Nz, int Nx,
+                              const double2 *d0_in, const double2 *dg_in,
+                              float2 *ex0, float2 *ex1, double2 *out) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    float2 D0[CPL], Dg[CPL];
+#pragma unroll
+    for (int i = 0; i < CPL; ++i) {
+        const int x = tid + i * nt;
+        D0[i] = make_float2(0.f, 0.f);
+        Dg[i] = make_float2(0.f, 0.f);
+        if (x < Nx) {
+            if (d0_in) {
+                const double2 v = d0_in[x];
+                D0[i] = make_float2((float)v.x, (float)v.y);
+            }
+            if (dg_in) {
+                const double2 v = dg_in[x];
+                Dg[i] = make_float2((float)v.x, (float)v.y);
+            }
+        }
+    }
+    for (int k = 0; k < Nz - 1; ++k) {
+        const float2 *cbk = cb + (size_t)k * Nx, *chk = ch + (size_t)k * Nx;
+#pragma unroll
+        for (int i = 0; i < CPL; ++i) {
+            const int x = tid + i * nt;
+            if (x < Nx) {
+                const float2 b = __ldg(cbk + x), h = __ldg(chk + x);
+                const float2 u = cadd(D0[i], cmulz(b, Dg[i]));
+                const float2 v = cmulz(csub(Dg[i], cmulz(h, D0[i])), ieg);
+                ex0[x + 1 == Nx ? 0 : x + 1] = cmulz(e0, u);
+                ex1[x == 0 ? Nx - 1 : x - 1] = v;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < CPL; ++i) {
+            const int x = tid + i * nt;
+            if (x < Nx) {
+                D0[i] = ex0[x];
+                Dg[i] = ex1[x];
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < CPL; ++i) {
+        const int x = tid + i * nt;
+        if (x < Nx) out[x] = make_double2(Dg[i].x, Dg[i].y);
+    }
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Mixed-radix Stockham FFT (Govindaraju et al., SC'08 formulation): stage of
 // radix R over butterflies j in [0, N/R), Ns = product of earlier radices;
@@ -150,14 +229,17 @@ struct FftPlan {
     int fac[24];
 };
 
-__device__ __forceinline__ double2 twid(const double2 *tw, int m, bool inv) {
-    double2 w = __ldg(tw + m);
+template <typename C>
+__device__ __forceinline__ C twid(const C *tw, int m, bool inv) {
+    C w = __ldg(tw + m);
     return inv ? cconj(w) : w;
 }
 
 // Returns the buffer holding the result (src or dst).  All threads call.
-__device__ double2 *fft_run(double2 *src, double2 *dst, const FftPlan &p,
-                            const double2 *__restrict__ tw, bool inv) {
+// C is double2 or float2 (the table tw has the same type).
+template <typename C>
+__device__ C *fft_run(C *src, C *dst, const FftPlan &p,
+                      const C *__restrict__ tw, bool inv) {
     const int N = p.n, tid = threadIdx.x, nt = blockDim.x;
     int Ns = 1;
     for (int f = 0; f < p.nfac; ++f) {
@@ -167,7 +249,7 @@ __device__ double2 *fft_run(double2 *src, double2 *dst, const FftPlan &p,
         if (R == 2) {
             for (int j = tid; j < nb; j += nt) {
                 const int k = j % Ns;
-                double2 a = src[j], b = src[j + nb];
+                C a = src[j], b = src[j + nb];
                 if (k) b = cmulz(b, twid(tw, k * step, inv));
                 const int d = (j / Ns) * Ns * 2 + k;
                 dst[d] = cadd(a, b);
@@ -176,18 +258,19 @@ __device__ double2 *fft_run(double2 *src, double2 *dst, const FftPlan &p,
         } else if (R == 4) {
             for (int j = tid; j < nb; j += nt) {
                 const int k = j % Ns;
-                double2 v0 = src[j], v1 = src[j + nb], v2 = src[j + 2 * nb],
-                        v3 = src[j + 3 * nb];
+                C v0 = src[j], v1 = src[j + nb], v2 = src[j + 2 * nb],
+                  v3 = src[j + 3 * nb];
                 if (k) {
                     v1 = cmulz(v1, twid(tw, k * step, inv));
                     v2 = cmulz(v2, twid(tw, 2 * k * step, inv));
                     v3 = cmulz(v3, twid(tw, 3 * k * step, inv));
                 }
-                const double2 s02 = cadd(v0, v2), d02 = csub(v0, v2);
-                const double2 s13 = cadd(v1, v3), d13 = csub(v1, v3);
+                const C s02 = cadd(v0, v2), d02 = csub(v0, v2);
+                const C s13 = cadd(v1, v3), d13 = csub(v1, v3);
                 // -i d13 forward, +i d13 inverse
-                const double2 rot = inv ? make_double2(-d13.y, d13.x)
-                                        : make_double2(d13.y, -d13.x);
+                C rot;
+                rot.x = inv ? -d13.y : d13.y;
+                rot.y = inv ? d13.x : -d13.x;
                 const int d = (j / Ns) * Ns * 4 + k;
                 dst[d] = cadd(s02, s13);
                 dst[d + Ns] = cadd(d02, rot);
@@ -201,7 +284,7 @@ __device__ double2 *fft_run(double2 *src, double2 *dst, const FftPlan &p,
                 // sum_r src[j + r nb] W^(r (k step + q nb))
                 int base = k * step + q * nb;
                 if (base >= N) base -= N;
-                double2 acc = src[j];
+                C acc = src[j];
                 int m = base;
                 for (int r = 1; r < R; ++r) {
                     acc = cadd(acc, cmulz(src[j + r * nb], twid(tw, m, inv)));
@@ -212,7 +295,7 @@ __device__ double2 *fft_run(double2 *src, double2 *dst, const FftPlan &p,
             }
         }
         __syncthreads();
-        double2 *t = src;
+        C *t = src;
         src = dst;
         dst = t;
         Ns *= R;
@@ -235,6 +318,28 @@ __device__ void precond_apply(double2 *w, double2 *a, double2 *b,
     double2 *g = fft_run(f, o, p, tw, true);
     const double inv_n = 1.0 / N;
     for (int x = tid; x < N; x += nt) w[x] = cscale(inv_n, g[x]);
+    __syncthreads();
+}
+
+// The same preconditioner in single precision: w (double) is rounded to
+// float, transformed with the float table, and widened back.  a, b: float2
+// scratch rows of N.
+__device__ void precond_apply32(double2 *w, float2 *a, float2 *b,
+                                const FftPlan &p,
+                                const float2 *__restrict__ tw,
+                                const float2 *__restrict__ iT) {
+    const int N = p.n, tid = threadIdx.x, nt = blockDim.x;
+    for (int x = tid; x < N; x += nt)
+        a[x] = make_float2((float)w[x].x, (float)w[x].y);
+    __syncthreads();
+    float2 *f = fft_run(a, b, p, tw, false);
+    for (int x = tid; x < N; x += nt) f[x] = cmulz(f[x], __ldg(iT + x));
+    __syncthreads();
+    float2 *o = f == a ? b : a;
+    float2 *g = fft_run(f, o, p, tw, true);
+    const double inv_n = 1.0 / N;
+    for (int x = tid; x < N; x += nt)
+        w[x] = make_double2(inv_n * g[x].x, inv_n * g[x].y);
     __syncthreads();
 }
 

@@ -163,7 +163,7 @@ typedef struct dyfox_bragg_desc {
     double beam_thickness, beam_centre;      /* top hat (BraggConfig)      */
     double tol;                              /* GMRES rtol (true residual) */
     int restart, maxiter;                    /* GMRES restart, maxiter     */
-    int precision;                           /* DYFOX_FP64                 */
+    int precision;                           /* DYFOX_FP64 / DYFOX_FP32    */
     unsigned flags;                          /* reserved, 0                */
 } dyfox_bragg_desc;
 
@@ -182,7 +182,13 @@ size_t dyfox_bragg_workspace_bytes(const dyfox_bragg_desc *d);
  * x0: device (n_s, n_y, Nx) complex128 warm start, or NULL for zero;
  * out: device (n_s, n_y, Nx) complex128; info: device (n_s * n_y, 4)
  * doubles per system: true relative residual, inner iterations, code (0
- * converged, else maxiter), |b|; or NULL. */
+ * converged, else maxiter), |b|; or NULL.
+ * precision DYFOX_FP32: mixed-precision solve.  The Arnoldi products (march
+ * and preconditioner) run in single precision; b, every true residual, the
+ * Gram-Schmidt coefficients, the rotations and the solution stay in double,
+ * so the stopping test is the same double-precision true residual <= tol.
+ * Inputs and outputs keep their complex128 layout.  The workspace grows by
+ * the single-precision couplings. */
 int dyfox_bragg_solve(const dyfox_bragg_desc *d, const double *seg_table,
                       const double *y_values, const double *s_dev,
                       const void *x0, void *out, double *info,
@@ -192,7 +198,8 @@ int dyfox_bragg_solve(const dyfox_bragg_desc *d, const double *seg_table,
  * mode 0: out = down-march of (D0(0), Dg(0)) = (in0, in1) to D_g(t)
  *         (bragg/solver.py:28-35; NULL input = zero);
  * mode 1: out = ifft(fft(in0) / T22s) (solver.py:167-168, 297-300).
- * in0, in1, out: device (n_s, n_y, Nx) complex128. */
+ * in0, in1, out: device (n_s, n_y, Nx) complex128.  precision DYFOX_FP32
+ * applies the single-precision operators of the mixed solve. */
 int dyfox_bragg_apply(const dyfox_bragg_desc *d, int mode,
                       const double *seg_table, const double *y_values,
                       const double *s_dev, const void *in0, const void *in1,

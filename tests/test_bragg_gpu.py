@@ -180,3 +180,77 @@ def test_bad_deviation_is_rejected(gpu, diamond400, small):
     b, cfg, seg, g = small
     with pytest.raises(ValueError):
         solve_surface_batch(seg, float("nan"), cfg, [0.0], diamond400, g)
+
+
+# --- the mixed-precision form (precision FP32) -----------------------------
+
+def test_mixed_operators_match_fp64(gpu, diamond400, small, rng):
+    """The single-precision march and preconditioner of the mixed solve
+    agree with their FP64 forms to <= 1e-5 relative L2 (float rounding over
+    Nz steps; the solve's accuracy does not rest on them)."""
+    from dyfox_gb300.bragg import apply_operator
+    torch = gpu
+    b, cfg, seg, g = small
+    s = [float(b["s_dev"]), -2e5]
+    ys = [0.0, 0.4e-6]
+    v = rng.normal(size=(2, 2, cfg.Nx)) + 1j * rng.normal(size=(2, 2, cfg.Nx))
+    w = rng.normal(size=(2, 2, cfg.Nx)) + 1j * rng.normal(size=(2, 2, cfg.Nx))
+    vt, wt = (torch.from_numpy(a).to("cuda") for a in (v, w))
+    for mode, kw in (("march", {"in0": wt, "in1": vt}),
+                     ("precond", {"in0": wt})):
+        hi = np_(apply_operator(seg, s, cfg, ys, diamond400, g, mode, **kw))
+        lo = np_(apply_operator(seg, s, cfg, ys, diamond400, g, mode, **kw,
+                                precision="fp32"))
+        assert 0 < rel_l2(lo, hi) < 1e-5, mode
+
+
+def test_mixed_solve_reaches_the_fp64_tolerance(gpu, diamond400, small):
+    """The mixed solve stops on the double-precision true residual: every
+    system converges to <= 1e-10 and the answer matches the FP64 solve and
+    the oracle's dense direct solve to <= 1e-8."""
+    from dyfox_gb300.bragg import solve_scan
+    b, cfg, seg, g = small
+    s = [float(b["s_dev"]), -1e5, 2e5]
+    ys = b["ys"]
+    o64, i64 = solve_scan(seg, s, cfg, ys, diamond400, g)
+    o32, i32 = solve_scan(seg, s, cfg, ys, diamond400, g, precision="fp32")
+    i32 = np_(i32)
+    assert i32[:, 0].max() < 1e-10 and np.all(i32[:, 2] == 0)
+    assert o32.dtype == gpu.complex128
+    o32, o64 = np_(o32), np_(o64)
+    assert rel_l2(o32, o64) < 1e-8
+    dense, _ = BO.dense_solve(seg, s[0], cfg, diamond400, g, y=float(ys[0]))
+    assert rel_l2(o32[0, 0], dense) < 1e-8
+
+
+def test_mixed_surface_batch_and_stable(gpu, diamond400, small):
+    """The drop-ins take precision=FP32 and return the FP64 answers to the
+    solve tolerance."""
+    from dyfox_gb300.bragg import solve_bragg_stable, solve_surface_batch
+    b, cfg, seg, g = small
+    sd = float(b["s_dev"])
+    out, info = solve_surface_batch(seg, sd, cfg, b["ys"], diamond400, g,
+                                    precision="fp32")
+    assert info["converged"] and info["residual"] < 1e-10
+    for j in range(len(b["ys"])):
+        assert np.abs(out[j] - b["surface"][j]).max() < \
+            1e-7 * np.abs(b["surface"][j]).max()
+    wave, inf = solve_bragg_stable(seg, sd, cfg, diamond400, g,
+                                   precision="fp32")
+    assert inf["gmres_code"] == 0 and inf["residual"] < 1e-10
+    assert rel_l2(wave, b["exit_wave"]) < 1e-7
+
+
+def test_mixed_config1_planes(gpu, diamond400):
+    """Config-1 geometry (Nx 456, Nz 90): mixed and FP64 solves of the same
+    systems agree to <= 1e-8; the mixed form needs no more restarts than
+    maxiter allows."""
+    from dyfox_gb300.bragg import solve_scan
+    from dyfox_gb300.workloads import bragg_config1
+    x, cfg, seg, s, ys, g = bragg_config1()
+    sel_s, sel_y = s[::5], ys[::8]
+    o64, i64 = solve_scan(seg, sel_s, cfg, sel_y, x, g)
+    o32, i32 = solve_scan(seg, sel_s, cfg, sel_y, x, g, precision="fp32")
+    i32 = np_(i32)
+    assert i32[:, 0].max() < 1e-10 and np.all(i32[:, 2] == 0)
+    assert rel_l2(np_(o32), np_(o64)) < 1e-8
