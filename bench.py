@@ -64,6 +64,9 @@ def parse():
                          "exit (a small, fixed case for ncu)")
     ap.add_argument("--no-bragg", action="store_true")
     ap.add_argument("--no-scan", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-sample", type=int, default=0,
+                    help="batched leg on the first N instances (0: all 512)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the launch-shape autotuner (use its cache or "
                          "the built-in choice)")
@@ -370,12 +373,193 @@ def run_ours(args):
         line["bragg"] = bragg_leg(args, rank, world)
     if not args.no_scan:
         line["laue_scan"] = scan_leg(args, world)
+    if not args.no_batched:
+        line["batched"] = batched_leg(args, world)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, grid, seg, s, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def _fp64_row_checks(W, outs, n_streams=16):
+    """Per Laue instance: plain FP64 solve of the central row at the first
+    and last deviation parameter (one fused launch each, spread over
+    streams, own workspaces), and the exit-intensity relative L2 of the
+    batch's row against it."""
+    import torch
+    from dyfox_gb300 import _lib
+    from dyfox_gb300.backend import FP64
+    from dyfox_gb300.grid import grid_arrays
+    from dyfox_gb300.laue import _desc
+    L = _lib.lib()
+    streams = [torch.cuda.Stream() for _ in range(n_streams)]
+    pend = []
+    for k, (w, out) in enumerate(zip(W, outs)):
+        x = w["xtal"]
+        geo = grid_arrays(w["grid"])
+        geo["fov_hy"] = 0.5 * geo["dx"]          # the row Ny / 2 only
+        sel = sorted({0, len(w["s"]) - 1})
+        tab = _lib.segment_table(w["segs"], x.g_vec, x.nu, x.a_core,
+                                 geo["dx"])
+        src = _lib.H_SEGMENTS if len(tab) else _lib.H_NONE
+        d = _desc(x, geo, len(sel), FP64, src, len(tab), None,
+                  _lib.FLAG_FUSED)
+        st = streams[k % n_streams]
+        with torch.cuda.stream(st):
+            table = _lib.device_table(tab) if len(tab) else None
+            sd = torch.tensor(np.asarray(w["s"])[sel], dtype=torch.float64,
+                              device="cuda")
+            ws = torch.empty(max(L.dyfox_laue_workspace_bytes(d), 256),
+                             dtype=torch.uint8, device="cuda")
+            ref = torch.empty((len(sel), geo["Ny"], geo["Nx"]),
+                              dtype=torch.complex128, device="cuda")
+            _lib.check(L.dyfox_laue_solve(
+                d, _lib.ptr(sd), None, _lib.ptr(table), _lib.ptr(ref),
+                _lib.ptr(ws), ws.numel(), _lib.c_void_p(st.cuda_stream)),
+                "dyfox_laue_solve")
+        pend.append((ref, out, sel, geo["Ny"] // 2, table, sd, ws))
+    torch.cuda.synchronize()
+    errs = []
+    for ref, out, sel, r, *_ in pend:
+        a = (out[sel, r].to(torch.complex128).abs() ** 2)
+        b = ref[:, r].abs() ** 2
+        errs.append(float(torch.linalg.vector_norm(a - b) /
+                          max(float(torch.linalg.vector_norm(b)), 1e-300)))
+    return errs
+
+
+def batched_leg(args, world):
+    """Batched uneven instances: 512 seeded instances (70% Laue, 30% Bragg),
+    one CUDA graph per replay (per-instance set-up, one persistent Laue
+    march launch, one Bragg launch).  Laue: compensated FP32 march with the
+    segment sum and 2 pi reduction in double (complex64 state, FP64 H);
+    Bragg: mixed-precision solve to true residual 1e-10.  Launch shape
+    from the batch autotuner.  Per-instance error against plain FP64 (Laue:
+    central row at the first and last angle; Bragg: every system); a
+    sample of the instances is also timed as plain FP64 single calls and as
+    FP32 single calls."""
+    import torch
+    from dyfox_gb300 import _lib
+    from dyfox_gb300.batch import Batch, autotune, from_workload
+    from dyfox_gb300.bragg import solve_scan
+    from dyfox_gb300.grid import grid_arrays
+    from dyfox_gb300.laue import solve_dislocation
+    from dyfox_gb300.workloads import batched_uneven
+    L = _lib.lib()
+    W = batched_uneven()
+    if args.batched_sample:
+        W = W[:args.batched_sample]
+    inst = from_workload(W)
+    t0 = time.perf_counter()
+    if args.no_tune:
+        tuned = {"cols_per_lane": 5, "warps": 8, "ms": None}
+    else:
+        tuned = autotune(inst, h_sum="fp64")
+    tune_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b = Batch(inst, cols_per_lane=tuned["cols_per_lane"],
+              warps=tuned["warps"], h_sum="fp64")
+    plan_s = time.perf_counter() - t0
+    for _ in range(2):
+        b.run()
+    torch.cuda.synchronize()
+    steps = 3
+    times = []
+    n0 = L.dyfox_launch_count()
+    for _ in range(steps):
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record()
+        b.run()
+        a1.record()
+        torch.cuda.synchronize()
+        times.append(a0.elapsed_time(a1))
+    launches = (L.dyfox_launch_count() - n0) // steps
+    ms = statistics.mean(times)
+    laue_vs, bragg_solves, bragg_sys = 0, 0, 0
+    for w in W:
+        if w["kind"] == "laue":
+            geo = grid_arrays(w["grid"])
+            rows = int(np.sum(np.abs((np.arange(geo["Ny"]) - geo["Ny"] // 2)
+                                     * geo["dx"]) < geo["fov_hy"]))
+            laue_vs += len(w["s"]) * rows * geo["Nx"] * (geo["Nz"] - 1)
+        else:
+            bragg_solves += len(w["s"])
+            bragg_sys += len(w["s"]) * len(w["ys"])
+    # per-instance error against FP64
+    li = [i for i, w in enumerate(W) if w["kind"] == "laue"]
+    bi = [i for i, w in enumerate(W) if w["kind"] == "bragg"]
+    t0 = time.perf_counter()
+    laue_err = _fp64_row_checks([W[i] for i in li], [b.outputs[i] for i in li])
+    bragg_err, bragg_res = [], []
+    for i in bi:
+        w = W[i]
+        ref, _ = solve_scan(w["segs"], w["s"], w["cfg"], w["ys"], w["xtal"],
+                            w["g"])
+        bragg_err.append(float(torch.linalg.vector_norm(b.outputs[i] - ref) /
+                               torch.linalg.vector_norm(ref)))
+        bragg_res.append(float(b.infos[i][:, 0].max()))
+    check_s = time.perf_counter() - t0
+    # a sample as single calls: plain FP64 and FP32
+    samp = li[:12] + bi[:6]
+    sub = Batch([inst[i] for i in samp], cols_per_lane=tuned["cols_per_lane"],
+                warps=tuned["warps"], h_sum="fp64")
+    sub.run()
+    torch.cuda.synchronize()
+
+    def wall(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) * 1e3
+
+    def singles(prec):
+        for i in samp:
+            w = W[i]
+            if w["kind"] == "laue":
+                solve_dislocation(w["segs"], w["s"], w["grid"], w["xtal"],
+                                  precision=prec,
+                                  h_sum="fp64" if prec == "fp32" else "ff")
+            else:
+                solve_scan(w["segs"], w["s"], w["cfg"], w["ys"], w["xtal"],
+                           w["g"], precision=prec)
+    sub_ms = wall(sub.run)
+    single32_ms = wall(lambda: singles("fp32"))
+    single64_ms = wall(lambda: singles("fp64"))
+    sec = ms * 1e-3
+    return {
+        "instances": len(W), "laue": len(li), "bragg": len(bi),
+        "ms_per_batch": ms, "instances_per_s": world * len(W) / sec,
+        "laue_voxel_steps_per_s": world * laue_vs / sec,
+        "laue_voxel_steps": laue_vs,
+        "bragg_solves_per_s": world * bragg_solves / sec,
+        "bragg_systems": bragg_sys,
+        "form": "one CUDA graph per replay: per-instance set-up, one "
+                "persistent Laue march launch (compensated FP32, segment sum "
+                "and 2 pi reduction in double, e^{iH} of each row evaluated "
+                "once by the CTA that marches it), one mixed-precision Bragg "
+                "launch",
+        "launch_shape": {"cols_per_lane": tuned["cols_per_lane"],
+                         "warps": tuned["warps"], "tuner_ms": tuned["ms"],
+                         "tuner_s": tune_s},
+        "plan_s": plan_s, "gpu_launches": int(launches),
+        "laue_intensity_rel_l2_vs_fp64": {
+            "max": max(laue_err) if laue_err else None,
+            "median": float(np.median(laue_err)) if laue_err else None,
+            "checked": "central row, first and last angle, every instance"},
+        "bragg_rel_l2_vs_fp64": {
+            "max": max(bragg_err) if bragg_err else None,
+            "median": float(np.median(bragg_err)) if bragg_err else None,
+            "max_true_residual": max(bragg_res) if bragg_res else None},
+        "fp64_checks_s": check_s,
+        "sample": {"instances": len(samp), "batched_ms": sub_ms,
+                   "fp32_single_calls_ms": single32_ms,
+                   "fp64_single_calls_ms": single64_ms,
+                   "timing": "host wall clock, synchronised"},
+    }
 
 
 def scan_leg(args, world):

@@ -28,26 +28,6 @@
 
 namespace dyfox {
 
-struct BraggArgs {
-    int Nx, Nz, n_y, n_s;
-    double ds, s0r, s0i, shr, shi, sbr, sbi;
-    const double *s_dev;          // (n_s)
-    const double2 *cb, *ch;       // (n_y, Nz, Nx): ds sigma e^{+-iH}
-    const double2 *e0h;           // (n_y, Nx): e^{-iH(z=0)}
-    const double2 *inc;           // (Nx): incident D0
-    const double2 *iT;            // (n_s, Nx): 1 / T22s
-    const double2 *tw;            // (Nx): exp(-2 pi i m / Nx)
-    const float2 *cb32, *ch32;    // FP32 copies of cb, ch (mixed form)
-    const float2 *iT32, *tw32;    // FP32 copies of iT, tw (mixed form)
-    FftPlan plan;
-    double2 *V;                   // (n_sys, m + 1, Nx)
-    double2 *Hh;                  // (n_sys, m, m + 1)
-    double2 *X, *B;               // (n_sys, Nx)
-    double2 *out;                 // (n_s, n_y, Nx)
-    double *info;                 // (n_sys, 4)
-    double tol;
-    int restart, maxiter, use_x0;
-};
 
 __device__ __forceinline__ void step_factors(const BraggArgs &a, int is,
                                              double2 &e0, double2 &ieg) {
@@ -204,9 +184,11 @@ __device__ void lartg(double2 f, double2 g, double &c, double2 &s,
 // cycle of the mixed form ends its inner iteration.
 constexpr double kMixedInnerDrop = 1e-5;
 
+// The solve of system `sys` (deviation parameter sys / n_y, plane
+// sys % n_y) of `a` by the calling CTA.  smem: gmres_smem(Nx, restart).
 template <int CPL, bool MIXED>
-__global__ void bragg_gmres_kernel(const BraggArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
+__device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
+                                             unsigned char *smem) {
     const int Nx = a.Nx, m = a.restart;
     double2 *A0 = reinterpret_cast<double2 *>(smem);
     double2 *A1 = A0 + Nx;
@@ -218,7 +200,7 @@ __global__ void bragg_gmres_kernel(const BraggArgs a) {
     double *gc = reinterpret_cast<double *>(gs + m);
     int *flags = reinterpret_cast<int *>(gc + m);          // [0] stop
 
-    const int sys = blockIdx.x, is = sys / a.n_y, iy = sys - is * a.n_y;
+    const int is = sys / a.n_y, iy = sys - is * a.n_y;
     const int tid = threadIdx.x, nt = blockDim.x;
     const double2 *cb = a.cb + (size_t)iy * a.Nz * Nx;
     const double2 *ch = a.ch + (size_t)iy * a.Nz * Nx;
@@ -448,6 +430,13 @@ __global__ void bragg_gmres_kernel(const BraggArgs a) {
     (void)flags;
 }
 
+// One CTA per system of one solve call.
+template <int CPL, bool MIXED>
+__global__ void bragg_gmres_kernel(const BraggArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    gmres_system<CPL, MIXED>(a, blockIdx.x, smem);
+}
+
 // Matvec / preconditioner for parity checks: one CTA per system.
 // mode 0: out = march(d0, dg); mode 1: out = M in.  MIXED: the
 // single-precision operators of the mixed form.
@@ -522,8 +511,8 @@ static int bragg_validate(const dyfox_bragg_desc *d) {
                   d->n_y, d->n_s, d->n_seg);
         return DYFOX_EINVAL;
     }
-    if (d->Nx > 16 * 512) {
-        set_error("Nx=%d above the supported 8192", d->Nx);
+    if (d->Nx > 16 * 256) {
+        set_error("Nx=%d above the supported 4096", d->Nx);
         return DYFOX_ENOSYS;
     }
     if (!(d->ds > 0) || !(d->dx > 0) || !(d->dz > 0) || !(d->tol > 0) ||
@@ -546,8 +535,10 @@ static int bragg_plan(const dyfox_bragg_desc *d, BraggPlan *p) {
     const size_t Nx = d->Nx, plane = (size_t)d->Nz * Nx * sizeof(double2);
     const size_t nsys = (size_t)d->n_y * d->n_s;
     const int m = d->restart;
-    // Columns per thread of the march: a power of two <= 8 for Nx <= 4096.
-    p->threads = Nx <= 512 ? 128 : (Nx <= 2048 ? 256 : 512);
+    // Columns per thread of the march: a power of two <= 16 (Nx <= 4096);
+    // 256 threads at most, so that the 16-column kernels (up to 255
+    // registers a thread) stay resident.
+    p->threads = Nx <= 512 ? 128 : 256;
     p->cpl = (int)((Nx + p->threads - 1) / p->threads);
     int c = 1;
     while (c < p->cpl) c *= 2;
@@ -589,10 +580,12 @@ __global__ void incident_kernel(double2 *inc, int Nx, double dx, int beam,
 }
 
 // Couplings, incident beam, twiddles and the preconditioner for `d`.
+// y_src: the planes' y, on the host (copied into the workspace), or on the
+// device when y_on_device.
 static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
-                         const double *seg_table, const double *y_host,
-                         const double *s_dev, char *ws, cudaStream_t stream,
-                         BraggArgs *a) {
+                         const double *seg_table, const double *y_src,
+                         bool y_on_device, const double *s_dev, char *ws,
+                         cudaStream_t stream, BraggArgs *a) {
     memset(a, 0, sizeof *a);
     a->Nx = d->Nx; a->Nz = d->Nz; a->n_y = d->n_y; a->n_s = d->n_s;
     a->ds = d->ds;
@@ -622,10 +615,14 @@ static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
     a->restart = d->restart;
     a->maxiter = d->maxiter;
     cudaError_t e;
-    double *y = (double *)(ws + p.off_y);
-    if ((e = cudaMemcpyAsync(y, y_host, sizeof(double) * d->n_y,
-                             cudaMemcpyHostToDevice, stream)))
-        return cuda_status(e, "y upload");
+    const double *y = y_src;
+    if (!y_on_device) {
+        double *yw = (double *)(ws + p.off_y);
+        if ((e = cudaMemcpyAsync(yw, y_src, sizeof(double) * d->n_y,
+                                 cudaMemcpyHostToDevice, stream)))
+            return cuda_status(e, "y upload");
+        y = yw;
+    }
     const long total = (long)d->n_y * d->Nz * d->Nx;
     long blocks = (total + 255) / 256;
     if (blocks > 152L * 64) blocks = 152L * 64;
@@ -646,6 +643,17 @@ static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
     return cuda_status(cudaGetLastError(), "bragg prepare");
 }
 
+// cudaErrorLaunchOutOfResources unless one CTA of `threads` threads and
+// `smem` bytes fits on an SM.
+template <typename K>
+static cudaError_t resident(K *k, int threads, size_t smem) {
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ, k, threads, smem);
+    if (e) return e;
+    return occ >= 1 ? cudaSuccess : cudaErrorLaunchOutOfResources;
+}
+
 template <int CPL, bool MIXED>
 static cudaError_t launch_gmres(const BraggArgs &a, int threads, size_t smem,
                                 int grid, cudaStream_t stream) {
@@ -655,6 +663,7 @@ static cudaError_t launch_gmres(const BraggArgs &a, int threads, size_t smem,
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e) return e;
     }
+    if (cudaError_t e = resident(k, threads, smem)) return e;
     k<<<grid, threads, smem, stream>>>(a);
     count_launch(1);
     return cudaGetLastError();
@@ -671,9 +680,119 @@ static cudaError_t launch_apply(const BraggArgs &a, int threads, size_t smem,
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e) return e;
     }
+    if (cudaError_t e = resident(k, threads, smem)) return e;
     k<<<grid, threads, smem, stream>>>(a, mode, d0, dg, out);
     count_launch(1);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Pieces used by the batched launcher (batch.cu): one CTA per system of
+// many instances, the instances' arguments in a device array.
+template <int CPL, bool MIXED>
+__global__ void bragg_batch_kernel(const BraggArgs *__restrict__ insts,
+                                   const int2 *__restrict__ systems) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ BraggArgs a;
+    const int2 w = systems[blockIdx.x];
+    if (threadIdx.x == 0) a = insts[w.x];
+    __syncthreads();
+    gmres_system<CPL, MIXED>(a, w.y, smem);
+}
+
+template <int CPL, bool MIXED>
+static cudaError_t launch_bragg_batch_t(const BraggArgs *insts,
+                                        const int2 *systems, int n_sys,
+                                        int threads, size_t smem,
+                                        cudaStream_t stream) {
+    bragg_batch_kernel<CPL, MIXED><<<n_sys, threads, smem, stream>>>(insts,
+                                                                   systems);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+template <int CPL, bool MIXED>
+static cudaError_t set_smem_t(size_t smem, int threads) {
+    cudaError_t e = cudaFuncSetAttribute(
+        bragg_batch_kernel<CPL, MIXED>,
+        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return e ? e : resident(bragg_batch_kernel<CPL, MIXED>, threads, smem);
+}
+
+// Dynamic shared memory of the batch kernel, and a check that one CTA fits
+// (before any launch or capture).
+cudaError_t set_bragg_batch_smem(int cpl, bool mixed, size_t smem,
+                                 int threads) {
+    switch (cpl * 2 + (mixed ? 1 : 0)) {
+    case 2: return set_smem_t<1, false>(smem, threads);
+    case 3: return set_smem_t<1, true>(smem, threads);
+    case 4: return set_smem_t<2, false>(smem, threads);
+    case 5: return set_smem_t<2, true>(smem, threads);
+    case 8: return set_smem_t<4, false>(smem, threads);
+    case 9: return set_smem_t<4, true>(smem, threads);
+    case 16: return set_smem_t<8, false>(smem, threads);
+    case 17: return set_smem_t<8, true>(smem, threads);
+    case 32: return set_smem_t<16, false>(smem, threads);
+    default: return set_smem_t<16, true>(smem, threads);
+    }
+}
+
+cudaError_t launch_bragg_batch(const BraggArgs *insts, const int2 *systems,
+                               int n_sys, int threads, int cpl, bool mixed,
+                               size_t smem, cudaStream_t stream) {
+    if (n_sys == 0) return cudaSuccess;
+#define DYFOX_BB(C, M) \
+    launch_bragg_batch_t<C, M>(insts, systems, n_sys, threads, smem, stream)
+    if (mixed) {
+        switch (cpl) {
+        case 1: return DYFOX_BB(1, true);
+        case 2: return DYFOX_BB(2, true);
+        case 4: return DYFOX_BB(4, true);
+        case 8: return DYFOX_BB(8, true);
+        default: return DYFOX_BB(16, true);
+        }
+    }
+    switch (cpl) {
+    case 1: return DYFOX_BB(1, false);
+    case 2: return DYFOX_BB(2, false);
+    case 4: return DYFOX_BB(4, false);
+    case 8: return DYFOX_BB(8, false);
+    default: return DYFOX_BB(16, false);
+    }
+#undef DYFOX_BB
+}
+
+// Workspace bytes, threads and columns per thread of one instance
+// (0 bytes: invalid descriptor, error set).
+size_t bragg_instance_bytes(const dyfox_bragg_desc *d, int *threads,
+                            int *cpl) {
+    BraggPlan p;
+    if (bragg_plan(d, &p)) return 0;
+    if (threads) *threads = p.threads;
+    if (cpl) *cpl = p.cpl;
+    return p.ws;
+}
+
+size_t bragg_instance_smem(const dyfox_bragg_desc *d) {
+    return gmres_smem(d->Nx, d->restart);
+}
+
+// Set-up kernels of one instance on `stream` (y already on the device) and
+// its arguments; out / info are the instance's results (info NULL: kept in
+// the workspace).
+int bragg_instance_prepare(const dyfox_bragg_desc *d, const double *seg_table,
+                           const double *y_dev, const double *s_dev,
+                           void *out, double *info, char *ws,
+                           cudaStream_t stream, BraggArgs *a) {
+    BraggPlan p;
+    int st = bragg_plan(d, &p);
+    if (st) return st;
+    if ((st = bragg_prepare(d, p, seg_table, y_dev, true, s_dev, ws, stream,
+                            a)))
+        return st;
+    a->out = (double2 *)out;
+    if (info) a->info = info;
+    return DYFOX_OK;
 }
 
 static int smem_ok(size_t need) {
@@ -723,7 +842,8 @@ extern "C" int dyfox_bragg_solve(const dyfox_bragg_desc *d,
     cudaStream_t stream = (cudaStream_t)stream_;
     char *ws = (char *)workspace;
     BraggArgs a;
-    if ((st = bragg_prepare(d, p, seg_table, y_values, s_dev, ws, stream, &a)))
+    if ((st = bragg_prepare(d, p, seg_table, y_values, false, s_dev, ws,
+                            stream, &a)))
         return st;
     const size_t nsys = (size_t)d->n_y * d->n_s;
     cudaError_t e;
@@ -788,7 +908,7 @@ extern "C" int dyfox_bragg_apply(const dyfox_bragg_desc *d, int mode,
     if ((st = smem_ok(smem))) return st;
     cudaStream_t stream = (cudaStream_t)stream_;
     BraggArgs a;
-    if ((st = bragg_prepare(d, p, seg_table, y_values, s_dev,
+    if ((st = bragg_prepare(d, p, seg_table, y_values, false, s_dev,
                             (char *)workspace, stream, &a)))
         return st;
     const int nsys = d->n_y * d->n_s;

@@ -304,7 +304,7 @@ __device__ C *fft_run(C *src, C *dst, const FftPlan &p,
 }
 
 // w <- ifft(fft(w) * iT) with iT = 1 / T22s; a, b are scratch rows.
-__device__ void precond_apply(double2 *w, double2 *a, double2 *b,
+__device__ inline void precond_apply(double2 *w, double2 *a, double2 *b,
                               const FftPlan &p,
                               const double2 *__restrict__ tw,
                               const double2 *__restrict__ iT) {
@@ -324,7 +324,7 @@ __device__ void precond_apply(double2 *w, double2 *a, double2 *b,
 // The same preconditioner in single precision: w (double) is rounded to
 // float, transformed with the float table, and widened back.  a, b: float2
 // scratch rows of N.
-__device__ void precond_apply32(double2 *w, float2 *a, float2 *b,
+__device__ inline void precond_apply32(double2 *w, float2 *a, float2 *b,
                                 const FftPlan &p,
                                 const float2 *__restrict__ tw,
                                 const float2 *__restrict__ iT) {
@@ -342,5 +342,28 @@ __device__ void precond_apply32(double2 *w, float2 *a, float2 *b,
         w[x] = make_double2(inv_n * g[x].x, inv_n * g[x].y);
     __syncthreads();
 }
+
+// Device-side arguments of the Bragg solve of one call (or one instance of
+// a batch): sizes, crystal, and pointers into the workspace.
+struct BraggArgs {
+    int Nx, Nz, n_y, n_s;
+    double ds, s0r, s0i, shr, shi, sbr, sbi;
+    const double *s_dev;          // (n_s)
+    const double2 *cb, *ch;       // (n_y, Nz, Nx): ds sigma e^{+-iH}
+    const double2 *e0h;           // (n_y, Nx): e^{-iH(z=0)}
+    const double2 *inc;           // (Nx): incident D0
+    const double2 *iT;            // (n_s, Nx): 1 / T22s
+    const double2 *tw;            // (Nx): exp(-2 pi i m / Nx)
+    const float2 *cb32, *ch32;    // FP32 copies of cb, ch (mixed form)
+    const float2 *iT32, *tw32;    // FP32 copies of iT, tw (mixed form)
+    FftPlan plan;
+    double2 *V;                   // (n_sys, m + 1, Nx)
+    double2 *Hh;                  // (n_sys, m, m + 1)
+    double2 *X, *B;               // (n_sys, Nx)
+    double2 *out;                 // (n_s, n_y, Nx)
+    double *info;                 // (n_sys, 4)
+    double tol;
+    int restart, maxiter, use_x0;
+};
 
 }  // namespace dyfox

@@ -42,6 +42,10 @@ void set_error(const char *fmt, ...);
 int cuda_status(cudaError_t e, const char *where);
 // Adds n to the launch counter read by dyfox_launch_count().
 void count_launch(unsigned n);
+// The counter's value, and setting it back (launches recorded into a CUDA
+// graph during stream capture run only when the graph is replayed).
+unsigned long long launch_count_value();
+void launch_count_restore(unsigned long long v);
 
 inline int div_up(int a, int b) { return (a + b - 1) / b; }
 

@@ -428,6 +428,38 @@ static int smem_limit(size_t need) {
     return DYFOX_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Pieces of a solve used by the batched launcher (batch.cu).
+int laue_check_desc(const dyfox_laue_desc *d) { return validate(d); }
+
+void laue_active_rows(const dyfox_laue_desc *d, int *row0, int *n_rows) {
+    active_rows(d, row0, n_rows);
+}
+
+cudaError_t launch_laue_setup(const dyfox_laue_desc *d, const double *s_dev,
+                              Kappa *kappa, float4 *kappa32, double2 *scale,
+                              cudaStream_t stream) {
+    const int nsteps = d->Nz - 1;
+    const long n = (long)d->n_e * nsteps;
+    laue_setup_kernel<<<(int)((n + 255) / 256), 256, 0, stream>>>(
+        s_dev, d->n_e, nsteps, d->ds, d->sig0[0], d->sig0[1], d->sig_h[0],
+        d->sig_h[1], d->sig_hbar[0], d->sig_hbar[1], kappa, kappa32, scale);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero_rows(const dyfox_laue_desc *d, void *out, size_t elem,
+                             int row0, int n_rows, cudaStream_t stream) {
+    if (n_rows >= d->Ny) return cudaSuccess;
+    const size_t row_bytes = (size_t)d->Nx * elem;
+    const long pairs = (long)d->n_e * (d->Ny - n_rows);
+    const int grid = pairs < 152L * 16 ? (int)pairs : 152 * 16;
+    zero_rows_kernel<<<grid, 256, 0, stream>>>((char *)out, d->n_e, d->Ny,
+                                               row_bytes, row0, n_rows);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
 }  // namespace dyfox
 
 using namespace dyfox;
@@ -489,27 +521,13 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
 
     cudaError_t e;
     // Rows outside the beam are zero.
-    if (p.n_rows < d->Ny) {
-        const size_t row_bytes = (size_t)d->Nx * elem;
-        const long pairs = (long)d->n_e * (d->Ny - p.n_rows);
-        const int grid = pairs < 152L * 16 ? (int)pairs : 152 * 16;
-        zero_rows_kernel<<<grid, 256, 0, stream>>>((char *)out, d->n_e, d->Ny,
-                                                   row_bytes, p.row0, p.n_rows);
-        count_launch(1);
-        if ((e = cudaGetLastError())) return cuda_status(e, "zero_rows");
-    }
+    if ((e = launch_zero_rows(d, out, elem, p.row0, p.n_rows, stream)))
+        return cuda_status(e, "zero_rows");
     if (p.n_rows == 0) return DYFOX_OK;
-
-    {
-        long n = (long)d->n_e * nsteps;
-        laue_setup_kernel<<<(int)((n + 255) / 256), 256, 0, stream>>>(
-            s_dev, d->n_e, nsteps, d->ds, d->sig0[0], d->sig0[1], d->sig_h[0],
-            d->sig_h[1], d->sig_hbar[0], d->sig_hbar[1],
-            (Kappa *)(ws + p.off_kappa), (float4 *)(ws + p.off_k32),
-            (double2 *)(ws + p.off_scale));
-        count_launch(1);
-        if ((e = cudaGetLastError())) return cuda_status(e, "laue_setup");
-    }
+    if ((e = launch_laue_setup(d, s_dev, (Kappa *)(ws + p.off_kappa),
+                               (float4 *)(ws + p.off_k32),
+                               (double2 *)(ws + p.off_scale), stream)))
+        return cuda_status(e, "laue_setup");
     if (p.hsrc == HS_SEG && single) {
         const long n = (long)p.n_rows * nsteps * d->n_seg;
         long blocks = (n + 255) / 256;

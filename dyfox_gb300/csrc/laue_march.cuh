@@ -215,18 +215,20 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// The march of one (row, angle group): row a.row0 + row_blk, deviation
+// parameters [grp * A, grp * A + A).  Every thread of the CTA calls it; the
+// CTA has 32 * WA * A threads or more (warps beyond WA * A idle).  smem: the
+// dynamic shared memory of march_smem's plan.
 template <typename R, int CPL, int HT, bool COMP>
-__global__ void laue_march_kernel(const MarchArgs a) {
+__device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
+                                            int grp, unsigned char *smem) {
     using R2 = typename RT<R>::R2;
-    extern __shared__ __align__(16) unsigned char smem[];
     const int WA = a.WA;
     const int nthreads = blockDim.x;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nwarps = nthreads >> 5;
     const int g = warp / WA, wa = warp - g * WA;
     const int L = wa * 32 + lane;
-    const int row_blk = blockIdx.x / a.n_groups;
-    const int grp = blockIdx.x - row_blk * a.n_groups;
     const int iy = a.row0 + row_blk;
     const int ie_raw = grp * a.A + g;
     const int ie = ie_raw < a.n_e ? ie_raw : a.n_e - 1;
@@ -547,6 +549,15 @@ __global__ void laue_march_kernel(const MarchArgs a) {
             out[x] = R2{(R)(S.x * br - S.y * bi), (R)(S.x * bi + S.y * br)};
         }
     }
+}
+
+// One CTA per (row, angle group) of one solve.
+template <typename R, int CPL, int HT, bool COMP>
+__global__ void laue_march_kernel(const MarchArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int row_blk = blockIdx.x / a.n_groups;
+    march_block<R, CPL, HT, COMP>(a, row_blk,
+                                  blockIdx.x - row_blk * a.n_groups, smem);
 }
 
 // Host launch of one instantiation; returns cudaError_t.  Also reports the

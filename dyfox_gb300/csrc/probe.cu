@@ -9,6 +9,8 @@ namespace dyfox {
 std::atomic<unsigned long long> g_launches{0};
 
 void count_launch(unsigned n) { g_launches += n; }
+unsigned long long launch_count_value() { return g_launches.load(); }
+void launch_count_restore(unsigned long long v) { g_launches.store(v); }
 
 // Eight independent FMA chains per thread, `iters` rounds each.
 template <typename R>

@@ -82,45 +82,8 @@ __global__ void cs_stage_kernel(const double *__restrict__ segs, int n_seg,
     const int iy = row0 + r;
     const int tid = threadIdx.x, nt = blockDim.x;
     if (SINGLE) {
-        SegF *segf = reinterpret_cast<SegF *>(smem);
-        float4 *piv = reinterpret_cast<float4 *>(smem + (size_t)n_seg * sizeof(SegF));
-        double *hc = reinterpret_cast<double *>(piv + (size_t)kStageKB * n_seg);
-        const double y_pix = (iy - Ny / 2) * dx;
-        if (tid == 0) *hc = sum_hconst(segs, n_seg);
-        for (int s = tid; s < n_seg; s += nt)
-            segf[s] = seg_f32(segs + (size_t)s * DYFOX_SEG_STRIDE);
-        for (int j = tid; j < kn * n_seg; j += nt) {
-            const int kb = j / n_seg, s = j - kb * n_seg;
-            piv[kb * n_seg + s] = seg_pivot(segs + (size_t)s * DYFOX_SEG_STRIDE,
-                                            y_pix, (k0 + kb) * dz, Nx, dx);
-        }
-        __syncthreads();
-        const double hconst = *hc;
-        const float hcr = reduce_2pi(hconst);
-        for (int j = tid; j < kn * Nx; j += nt) {
-            const int kb = j / Nx, x = j - kb * Nx;
-            const float4 *pv = piv + (size_t)kb * n_seg;
-            float ph;
-            if (SUM64) {
-                double acc = hconst;
-                for (int s = 0; s < n_seg; ++s)
-                    acc += (double)h_seg_f32(segf[s], pv[s], x);
-                ph = reduce_2pi(acc);
-            } else {
-                float hi = hcr, lo = 0.0f;
-                for (int s = 0; s < n_seg; ++s) {
-                    const float h = h_seg_f32(segf[s], pv[s], x);
-                    const float sum = hi + h, bb = sum - hi;
-                    lo += (hi - (sum - bb)) + (h - bb);
-                    hi = sum;
-                }
-                ph = reduce_2pi_ff(hi, lo);
-            }
-            float sn, c;
-            __sincosf(ph, &sn, &c);           // ph within [-pi, pi]
-            ((float2 *)out)[((size_t)r * nsteps + k0 + kb) * Nx + x] =
-                make_float2(c, sn);
-        }
+        stage_chunk32(segs, n_seg, Nx, Ny, dx, dz, iy, k0, kn, SUM64,
+                      (float2 *)out + (size_t)r * nsteps * Nx, smem);
     } else {
         const double yv = __dmul_rn((double)iy - 0.5 * Ny, dx);
         for (int j = tid; j < kn * Nx; j += nt) {
@@ -168,8 +131,7 @@ cudaError_t launch_cs_stage(bool single, bool sum64, const double *segs,
     const long grid = (long)n_rows * kchunks;
     if (grid == 0) return cudaSuccess;
     if (single) {
-        size_t smem = (size_t)n_seg * sizeof(SegF) +
-                      (size_t)kStageKB * n_seg * sizeof(float4) + sizeof(double);
+        size_t smem = stage_chunk32_smem(n_seg, kStageKB);
         auto *k = sum64 ? cs_stage_kernel<true, true> : cs_stage_kernel<true, false>;
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(

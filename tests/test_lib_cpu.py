@@ -129,3 +129,43 @@ def test_solvers_fail_loudly_without_a_gpu(diamond400, small_grid):
     from dyfox_gb300.laue import solve_pristine
     with pytest.raises(RuntimeError, match="CUDA"):
         solve_pristine([0.0], small_grid, diamond400)
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of the header's structs have the C compiler's
+    sizes and field offsets (a C program built from the header prints
+    them)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from dyfox_gb300 import _lib
+    from dyfox_gb300.batch import BatchItem, BatchOpts
+    from dyfox_gb300.bragg import BraggDesc
+    structs = {"dyfox_laue_desc": _lib.LaueDesc,
+               "dyfox_bragg_desc": BraggDesc,
+               "dyfox_batch_item": BatchItem,
+               "dyfox_batch_opts": BatchOpts}
+    lines = ['#include <stdio.h>', '#include <stddef.h>',
+             '#include "dyfox_gb300.h"', 'int main(void) {']
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'printf("{cname} {f[0]} %zu\\n", '
+                         f'offsetof({cname}, {f[0]}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-I", os.path.join(ROOT, "include"),
+                           str(src), "-o", str(exe)])
+    got = {}
+    for line in subprocess.check_output([str(exe)], text=True).splitlines():
+        cname, field, v = line.split()
+        got[(cname, field)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, \
+                (cname, f[0])
