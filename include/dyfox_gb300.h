@@ -212,6 +212,130 @@ int dyfox_bragg_apply(const dyfox_bragg_desc *d, int mode,
 int dyfox_bragg_symbol(const dyfox_bragg_desc *d, const double *s_dev,
                        void *T21, void *T22, void *stream);
 
+/* ---- Batched uneven instances --------------------------------------------
+ * No single DYFOX counterpart: a set of independent Laue and Bragg solves of
+ * different sizes (what a caller would otherwise issue as one
+ * solve_dislocation / solve_surface_batch call per instance) planned once
+ * and replayed as one CUDA graph:
+ *   * every Laue instance's per-angle set-up, then ONE persistent march
+ *     launch over a cost-sorted queue of (instance, row) items: the CTA that
+ *     takes an item stages e^{iH} of that row once into its own slab and
+ *     marches every angle group of the instance through it;
+ *   * every Bragg instance's couplings / symbol set-up, then ONE launch of
+ *     one CTA per (instance, deviation parameter, plane) system, longest
+ *     first (one launch per precision present).
+ * Laue items: precision DYFOX_FP32 (compensated march), h_source
+ * DYFOX_H_SEGMENTS or DYFOX_H_NONE, shift_px == 1, Nx even and at most
+ * 32 * cols_per_lane * warps; flags DYFOX_FLAG_H_FP64 sums the segment
+ * terms and reduces mod 2 pi in double (else float-float).  Output
+ * (n_e, Ny, Nx) complex64.  Bragg items: as dyfox_bragg_solve (either
+ * precision; x0 = 0), output (n_s, n_y, Nx) complex128, y_values on the
+ * HOST (uploaded by dyfox_batch_create). */
+#define DYFOX_BATCH_LAUE 0
+#define DYFOX_BATCH_BRAGG 1
+
+typedef struct dyfox_batch_item {
+    int kind;                     /* DYFOX_BATCH_LAUE / DYFOX_BATCH_BRAGG     */
+    dyfox_laue_desc laue;         /* kind LAUE                                */
+    dyfox_bragg_desc bragg;       /* kind BRAGG                               */
+    const double *s_dev;          /* device: n_e (Laue) / n_s (Bragg)         */
+    const double *seg_table;      /* device: n_seg x DYFOX_SEG_STRIDE, or NULL*/
+    const double *y_values;       /* BRAGG: HOST, n_y doubles                 */
+    void *out;                    /* device output (see above)                */
+    double *info;                 /* BRAGG: device (n_s * n_y, 4), or NULL    */
+} dyfox_batch_item;
+
+typedef struct dyfox_batch_opts {
+    int laue_cols_per_lane;       /* 5, 7, 9 or 11; 0: 5                     */
+    int laue_warps;               /* warps per CTA of the Laue march: 4, 8 or
+                                     16; 0: 8                                 */
+    int laue_ctas_per_sm;         /* resident CTAs per SM; 0: occupancy max   */
+    unsigned flags;               /* DYFOX_FLAG_H_FP64                        */
+} dyfox_batch_opts;
+
+typedef struct dyfox_batch dyfox_batch;     /* opaque plan + CUDA graph */
+
+/* Workspace bytes of a batch into *bytes; a status (invalid or unsupported
+ * items: see dyfox_last_error). */
+int dyfox_batch_workspace_bytes(const dyfox_batch_item *items, int n,
+                                const dyfox_batch_opts *opts, size_t *bytes);
+
+/* Plans the batch, uploads its tables (synchronously, on `stream`), and
+ * captures and instantiates its CUDA graph.  The workspace, items' inputs
+ * and outputs must stay valid until dyfox_batch_destroy; opts may be NULL. */
+int dyfox_batch_create(const dyfox_batch_item *items, int n,
+                       const dyfox_batch_opts *opts, void *workspace,
+                       size_t workspace_bytes, void *stream,
+                       dyfox_batch **batch);
+
+/* Replays the batch's graph on `stream` (asynchronous). */
+int dyfox_batch_launch(dyfox_batch *batch, void *stream);
+
+/* Kernel launches one replay makes (the graph's kernel nodes). */
+int dyfox_batch_kernel_count(const dyfox_batch *batch);
+
+/* Frees the graph and the plan (not the workspace). */
+int dyfox_batch_destroy(dyfox_batch *batch);
+
+/* ---- Learned shooting guess (no DYFOX counterpart) ------------------------
+ * A 4-level U-Net, 32 base channels, bfloat16 storage and FP32 accumulation
+ * (the 3x3 convolutions are implicit GEMMs on the tensor cores), mapping
+ * (cos, sin) of H on the first 8 depth slices of a set of y-planes plus the
+ * deviation parameter (input (n, H, W, 32) bf16, channels 17..31 zero) to
+ * the shooting unknown D_g(0) minus its perfect-crystal value ((n, H, W, 2)
+ * float32, Re and Im).  The Bragg solve takes it as x0 (dyfox_bragg_solve)
+ * and keeps its own residual test.  Parameters: FP32, flat, in the order of
+ * the layer list (per 3x3 convolution W[Cout][3][3][Cin] then b[Cout]:
+ * e0a e0b e1a e1b e2a e2b ba bb d2a d2b d1a d1b d0a d0b; then the 1x1 head
+ * W[2][32], b[2]).  All buffers live in one caller workspace (256-byte
+ * aligned). */
+typedef struct dyfox_unet dyfox_unet;
+
+size_t dyfox_unet_param_count(void);
+int dyfox_unet_workspace_bytes(int batch, int H, int W, size_t *bytes);
+int dyfox_unet_create(int batch, int H, int W, void *workspace,
+                      size_t workspace_bytes, dyfox_unet **net);
+int dyfox_unet_destroy(dyfox_unet *net);
+/* Device pointers of the FP32 parameters and of their gradients. */
+int dyfox_unet_params(dyfox_unet *net, float **params, float **grads);
+/* He-normal weights from a counter-based generator, zero biases and Adam
+ * state. */
+int dyfox_unet_init(dyfox_unet *net, unsigned long long seed, void *stream);
+/* Refresh the bfloat16 weight copies after the FP32 parameters changed. */
+int dyfox_unet_refresh(dyfox_unet *net, void *stream);
+/* Forward pass of n <= batch samples; y (device, may be NULL) receives the
+ * (n, H, W, 2) output.  Keeps the activations for dyfox_unet_backward. */
+int dyfox_unet_forward(dyfox_unet *net, const void *x, int n, float *y,
+                       void *stream);
+/* Gradients of L = sum((y - t)^2) / (2 * 2 n H W) after a forward pass;
+ * loss (device float, may be NULL) receives L. */
+int dyfox_unet_backward(dyfox_unet *net, const float *target, float *loss,
+                        void *stream);
+/* One Adam step on the gradients, then refresh of the bfloat16 copies. */
+int dyfox_unet_adam(dyfox_unet *net, float lr, float beta1, float beta2,
+                    float eps, void *stream);
+/* Network input from the top 8 depth slices of H: h_top (n_y, 8, Nx)
+ * doubles, columns [col0, col0 + W), s_values (n_s doubles, already
+ * scaled); x_out (n_s, n_y, W, 32) bfloat16. */
+int dyfox_unet_features(const double *h_top, int n_y, int Nx, int col0,
+                        int W, const double *s_values, int n_s, void *x_out,
+                        void *stream);
+/* Device buffer of the last forward / backward pass, for checks: which 0
+ * conv output `index` (bf16), 1 pooled tensor (bf16), 2 concatenated input
+ * of d2a / d1a / d0a (bf16), 3 gradient of conv output `index` (float);
+ * sized for the network's batch, NHWC. */
+int dyfox_unet_buffer(dyfox_unet *net, int which, int index, void **ptr,
+                      size_t *bytes);
+/* One 3x3 convolution product, for checks: mode 0 out = bf16(relu(conv(X,
+ * Wk) + bias)) (Wk [Cout][9][Cin]); mode 1 out = data gradient of G
+ * (float, (N, H, W, Cin); Wk the transposed weights [Cin][9][Cout]); mode
+ * 2 out = weight gradient [Cout][9][Cin] (float) of X and G, with the
+ * split partials in the workspace.  Channels multiples of 32. */
+int dyfox_unet_conv(int mode, const void *X, const void *G, const void *Wk,
+                    const float *bias, void *out, int N, int H, int W,
+                    int Cin, int Cout, void *workspace,
+                    size_t workspace_bytes, void *stream);
+
 /* Diagnostic (not part of any DYFOX interface): measured FMA throughput
  * of this GPU in TFLOP/s (2 flops per FMA) for DYFOX_FP64 or DYFOX_FP32,
  * the denominator of the arithmetic-bound kernels' roofline.  Synchronises

@@ -1,0 +1,216 @@
+"""The U-Net training and inference kernels against the NumPy oracle
+(oracle/unet_oracle.py, pinned by finite differences).
+
+Tight checks: each tensor-core product (forward, data gradient, weight
+gradient of a 3x3 convolution) alone against FP64 on the same bfloat16
+operands, and every layer of a full forward + backward pass against the
+oracle evaluated on the GPU's own input to that layer.  Bfloat16 outputs
+equal the correctly rounded FP64 value except where FP32 accumulation
+lands on the other side of a rounding midpoint (<= 2e-3 of the elements,
+never more than one unit in the last place); FP32 products agree to
+<= 1e-5 relative L2.
+
+Chained check: the whole network against the oracle run end to end.  An
+isolated rounding flip in one layer moves that element by one bfloat16
+unit, and a 14-layer ReLU network carries such perturbations forward
+(measured: one flipped element of e1b grows to 2e-3 relative at the
+output), so this integration check allows 2e-2 on the output and 0.15 on
+the gradients.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from oracle import unet_oracle as U
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(rng, n=2, H=16, W=16, seed=2):
+    p = U.init_params(seed=seed)
+    for k in p:
+        if k.endswith(".b"):
+            p[k] = rng.normal(size=p[k].shape) * 0.05
+    flat32 = U.flatten(p).astype(np.float32)
+    p32 = U.unflatten(flat32.astype(np.float64))
+    x = U.bf16(rng.normal(size=(n, H, W, U.C_IN)))
+    x[..., 17:] = 0.0
+    t = rng.normal(size=(n, H, W, 2)).astype(np.float32)
+    return p32, flat32, x, t
+
+
+@pytest.mark.parametrize("N,H,W,Cin,Cout", [(2, 16, 12, 32, 32),
+                                            (1, 8, 8, 96, 64),
+                                            (3, 12, 20, 64, 128)])
+def test_single_conv_products(gpu, rng, N, H, W, Cin, Cout):
+    from dyfox_gb300.learned import conv
+    torch = gpu
+
+    def dev_bf16(a):
+        return torch.tensor(a, dtype=torch.float32).to(torch.bfloat16).cuda()
+    X = U.bf16(rng.normal(size=(N, H, W, Cin)))
+    G = U.bf16(rng.normal(size=(N, H, W, Cout)))
+    Wt = U.bf16(rng.normal(size=(Cout, 3, 3, Cin)) * 0.1)
+    b = rng.normal(size=Cout).astype(np.float32)
+    # forward: one bfloat16 rounding of relu(conv + b)
+    y = conv("fwd", X=dev_bf16(X), Wk=dev_bf16(Wt), bias=torch.tensor(b).cuda(),
+             Cout=Cout).float().cpu().numpy()
+    ref = np.maximum(U.conv3(X, Wt, b.astype(np.float64)), 0.0)
+    assert np.all(np.abs(y - ref) <= 2.0 ** -7 * np.abs(ref) + 1e-30)
+    assert np.mean(y != U.bf16(ref)) <= 2e-3
+    # data and weight gradients: FP32 accumulation of exact products
+    dx_ref, dw_ref, _ = U.conv3_backward(X, Wt, G)
+    WtT = np.ascontiguousarray(np.transpose(Wt, (3, 1, 2, 0)))   # [ci][ky][kx][co]
+    dx = conv("dgrad", G=dev_bf16(G), Wk=dev_bf16(WtT), Cin=Cin,
+              Cout=Cout).cpu().numpy()
+    assert rel_l2(dx, dx_ref) < 1e-5
+    dw = conv("wgrad", X=dev_bf16(X), G=dev_bf16(G)).cpu().numpy()
+    assert rel_l2(dw.reshape(Cout, 3, 3, Cin), dw_ref) < 1e-5
+
+
+def _conv_in(net, i, x, n):
+    if i == 0:
+        return x
+    if i in (2, 4, 6):
+        return net.buffer("pool", i // 2 - 1, n).cpu().numpy()
+    if i in (8, 10, 12):
+        return net.buffer("cat", (i - 8) // 2, n).cpu().numpy()
+    return net.buffer("act", i - 1, n).cpu().numpy()
+
+
+def test_layerwise_against_the_oracle(gpu, rng):
+    """Every layer of one forward and backward pass against the oracle
+    evaluated on the GPU's own inputs to that layer (no error carried over
+    from earlier layers): bfloat16 outputs within one rounding, FP32
+    products within 1e-5."""
+    from dyfox_gb300.learned import UNet
+    torch = gpu
+    n, H, W = 2, 16, 16
+    p32, flat32, x, t = _setup(rng, n, H, W)
+    net = UNet(batch=n, H=H, W=W)
+    net.load(flat32)
+    y = net.forward(torch.tensor(x, dtype=torch.float32).to(
+        torch.bfloat16).cuda()).cpu().numpy()
+    net.backward(torch.tensor(t).cuda())
+    grads = U.unflatten(net.grads.cpu().numpy().astype(np.float64))
+    names = [c[0] for c in U.CONVS]
+    for i, name in enumerate(names):
+        xin = _conv_in(net, i, x, n)
+        Wr = U.bf16(p32[name + ".W"])
+        ref = np.maximum(U.conv3(xin, Wr, p32[name + ".b"]), 0.0)
+        got = net.buffer("act", i, n).cpu().numpy()
+        assert np.all(np.abs(got - ref) <= 2.0 ** -7 * np.abs(ref) + 1e-30), \
+            (name, float(np.abs(got - ref).max()))
+        assert np.mean(got != U.bf16(ref)) <= 2e-3, name
+    for l in range(3):
+        src = net.buffer("act", 2 * l + 1, n).cpu().numpy()
+        got = net.buffer("pool", l, n).cpu().numpy()
+        assert np.array_equal(got, U.bf16(U.pool(src))), l
+    for c, (lo, sk) in enumerate(((7, 5), (9, 3), (11, 1))):
+        ref = np.concatenate([U.up(net.buffer("act", lo, n).cpu().numpy()),
+                              net.buffer("act", sk, n).cpu().numpy()], -1)
+        assert np.array_equal(net.buffer("cat", c, n).cpu().numpy(), ref), c
+    d0 = net.buffer("act", 13, n).cpu().numpy()
+    yref = d0 @ p32["head.W"].T + p32["head.b"]
+    assert rel_l2(y, yref) < 1e-6
+    dy = (y - t) / y.size
+    assert rel_l2(net.buffer("dout", 13, n).cpu().numpy(),
+                  dy @ p32["head.W"]) < 1e-5
+    assert rel_l2(grads["head.W"], np.einsum("nyxc,nyxi->ci", dy, d0)) < 1e-5
+    for i, name in enumerate(names):
+        xin = _conv_in(net, i, x, n)
+        act = net.buffer("act", i, n).cpu().numpy()
+        G = U.bf16(net.buffer("dout", i, n).cpu().numpy() * (act > 0))
+        dx, dW, db = U.conv3_backward(xin, U.bf16(p32[name + ".W"]), G)
+        assert rel_l2(grads[name + ".W"], dW) < 1e-5, name
+        assert rel_l2(grads[name + ".b"], db) < 1e-5, name
+        if i > 0 and i not in (2, 4, 6, 8, 10, 12):
+            assert rel_l2(net.buffer("dout", i - 1, n).cpu().numpy(),
+                          dx) < 1e-5, name
+
+
+@pytest.mark.parametrize("shape", [(2, 16, 16), (3, 32, 24)])
+def test_forward_and_gradients_match_the_oracle(gpu, rng, shape):
+    from dyfox_gb300.learned import UNet
+    torch = gpu
+    n, H, W = shape
+    p32, flat32, x, t = _setup(rng, n, H, W)
+    net = UNet(batch=4, H=H, W=W)
+    assert net.n_params == U.n_params()
+    net.load(flat32)
+    xt = torch.tensor(x, dtype=torch.float32).to(torch.bfloat16).cuda()
+    y = net.forward(xt)
+    loss = net.backward(torch.tensor(t).cuda())
+    yo, cache = U.forward(p32, x, bf16_storage=True)
+    go = U.backward(p32, cache, yo, t.astype(np.float64), bf16_storage=True)
+    assert rel_l2(y.cpu().numpy(), yo) < 2e-2
+    assert float(loss) == pytest.approx(U.loss(yo, t), rel=2e-2)
+    gg = U.unflatten(net.grads.cpu().numpy().astype(np.float64))
+    for name, _ in U.param_layout():
+        assert rel_l2(gg[name], go[name]) < 0.15, name
+
+
+def test_adam_step_matches_numpy(gpu, rng):
+    from dyfox_gb300.learned import UNet
+    torch = gpu
+    p32, flat32, x, t = _setup(rng)
+    net = UNet(batch=2, H=16, W=16)
+    net.load(flat32)
+    net.forward(torch.tensor(x, dtype=torch.float32).to(torch.bfloat16).cuda())
+    net.backward(torch.tensor(t).cuda())
+    g = net.grads.cpu().numpy().astype(np.float64)
+    net.step(lr=1e-3)
+    m = 0.1 * g
+    v = 0.001 * g * g
+    want = flat32 - 1e-3 * (m / 0.1) / (np.sqrt(v / 0.001) + 1e-8)
+    got = net.params.cpu().numpy()
+    assert np.allclose(got, want, rtol=1e-5, atol=1e-7)
+
+
+def test_training_reduces_the_loss(gpu, rng):
+    """A learnable map (target = functions of the input channels): the
+    loss falls by 5x within a few hundred Adam steps."""
+    from dyfox_gb300.learned import UNet
+    torch = gpu
+    n, H, W = 16, 32, 32
+    x = U.bf16(rng.normal(size=(n, H, W, U.C_IN)) * 0.5)
+    x[..., 17:] = 0.0
+    t = np.stack([x[..., 0] - 0.5 * x[..., 3],
+                  np.tanh(x[..., 16]) * x[..., 1]], axis=-1)
+    X = torch.tensor(x, dtype=torch.float32).to(torch.bfloat16).cuda()
+    T = torch.tensor(t, dtype=torch.float32).cuda()
+    net = UNet(batch=4, H=H, W=W, seed=5)
+    hist = net.train(X, T, epochs=60, lr=2e-3)
+    assert hist[-1] < 0.2 * hist[0]
+    assert np.all(np.isfinite(hist))
+
+
+def test_features(gpu, rng):
+    from dyfox_gb300.learned import features
+    torch = gpu
+    h = rng.normal(size=(5, 8, 40)) * 4
+    s = np.array([0.3, -1.2])
+    got = features(torch.tensor(h).cuda(), 6, 24, s).float().cpu().numpy()
+    assert got.shape == (2, 5, 24, 32)
+    win = h[:, :, 6:30]
+    for k in range(8):
+        assert np.array_equal(got[..., 2 * k],
+                              np.broadcast_to(U.bf16(np.cos(win[:, k])),
+                                              (2, 5, 24)))
+        assert np.array_equal(got[..., 2 * k + 1],
+                              np.broadcast_to(U.bf16(np.sin(win[:, k])),
+                                              (2, 5, 24)))
+    assert np.array_equal(got[0, ..., 16], np.full((5, 24), U.bf16(0.3)))
+    assert np.all(got[..., 17:] == 0)
+
+
+def test_bad_shapes(gpu):
+    from dyfox_gb300.learned import UNet
+    torch = gpu
+    with pytest.raises(ValueError):
+        UNet(batch=1, H=20, W=16)
+    net = UNet(batch=1, H=16, W=16)
+    with pytest.raises(ValueError):
+        net.forward(torch.zeros((2, 16, 16, 32), dtype=torch.bfloat16,
+                                device="cuda"))
