@@ -88,6 +88,19 @@ def active_rows(geo):
     return iy[np.abs((iy - geo["Ny"] // 2) * geo["dx"]) < geo["fov_hy"]]
 
 
+def max_over_ranks(t_local, world):
+    """The largest of every rank's ``t_local`` (a time in seconds); the
+    value itself for one rank.  Works on the NCCL (CUDA tensor) and gloo
+    (CPU tensor) backends."""
+    if world <= 1:
+        return float(t_local)
+    import torch
+    dev = "cuda" if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(t_local)], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t)
+
+
 def dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -290,11 +303,7 @@ def run_ours(args):
     err_sum64 = float(torch.linalg.vector_norm(I32b - I64)
                       / torch.linalg.vector_norm(I64))
 
-    tot = sum(ms) / 1e3
-    if world > 1:
-        t = torch.tensor([tot], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tot = float(t)
+    tot = max_over_ranks(sum(ms) / 1e3, world)
     value = world * units * args.steps / tot
     mean_ms = 1e3 * tot / args.steps
     plain_ms = statistics.mean(ms_plain)
@@ -477,7 +486,7 @@ def batched_leg(args, world):
         torch.cuda.synchronize()
         times.append(a0.elapsed_time(a1))
     launches = (L.dyfox_launch_count() - n0) // steps
-    ms = statistics.mean(times)
+    ms = 1e3 * max_over_ranks(statistics.mean(times) * 1e-3, world)
     laue_vs, bragg_solves, bragg_sys = 0, 0, 0
     for w in W:
         if w["kind"] == "laue":
@@ -612,7 +621,7 @@ def scan_leg(args, world):
     I64 = ref.abs() ** 2
     err = float(torch.linalg.vector_norm(I32 - I64)
                 / torch.linalg.vector_norm(I64))
-    ms = statistics.mean(times)
+    ms = 1e3 * max_over_ranks(statistics.mean(times) * 1e-3, world)
     return {"value": world * units / (ms * 1e-3), "unit": "voxel-steps/s",
             "ms_per_scan": ms, "voxel_steps_per_scan": units,
             "angles": len(s), "segments": len(segs), "active_rows":
@@ -660,6 +669,8 @@ def bragg_leg(args, rank, world):
 
     o32, inf, ms, launches = timed("fp32")
     o64, inf64, ms64, _ = timed("fp64")
+    ms = 1e3 * max_over_ranks(ms * 1e-3, world)
+    ms64 = 1e3 * max_over_ranks(ms64 * 1e-3, world)
     diff = float(torch.linalg.vector_norm(o32 - o64) /
                  torch.linalg.vector_norm(o64))
     res = {"value": world * len(s) / (ms * 1e-3), "unit": "Bragg solves/s",
