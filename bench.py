@@ -65,6 +65,15 @@ def parse():
     ap.add_argument("--no-bragg", action="store_true")
     ap.add_argument("--no-scan", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-train", type=int, default=8,
+                    help="training instances of the learned-guess leg "
+                         "(64 solves each)")
+    ap.add_argument("--learned-test", type=int, default=2)
+    ap.add_argument("--learned-epochs", type=int, default=6)
+    ap.add_argument("--learned-tmax", type=float, default=40e-6,
+                    help="thickest instance of the learned-guess leg (m); "
+                         "the configuration's range ends at 100e-6")
     ap.add_argument("--batched-sample", type=int, default=0,
                     help="batched leg on the first N instances (0: all 512)")
     ap.add_argument("--no-tune", action="store_true",
@@ -384,6 +393,8 @@ def run_ours(args):
         line["laue_scan"] = scan_leg(args, world)
     if not args.no_batched:
         line["batched"] = batched_leg(args, world)
+    if not args.no_learned:
+        line["learned_guess"] = learned_leg(args, world)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, grid, seg, s, args.cpu_seconds)
     if rank == 0:
@@ -497,9 +508,30 @@ def batched_leg(args, world):
         else:
             bragg_solves += len(w["s"])
             bragg_sys += len(w["s"]) * len(w["ys"])
-    # per-instance error against FP64
     li = [i for i, w in enumerate(W) if w["kind"] == "laue"]
     bi = [i for i, w in enumerate(W) if w["kind"] == "bragg"]
+    # the two parts alone (each its own graph)
+    part_ms = {}
+    for key, idx in (("laue", li), ("bragg", bi)):
+        if not idx:
+            continue
+        pb = Batch([inst[i] for i in idx],
+                   cols_per_lane=tuned["cols_per_lane"],
+                   warps=tuned["warps"], h_sum="fp64")
+        pb.run()
+        torch.cuda.synchronize()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record()
+        for _ in range(2):
+            pb.run()
+        a1.record()
+        torch.cuda.synchronize()
+        part_ms[key] = 1e3 * max_over_ranks(a0.elapsed_time(a1) * 5e-4,
+                                            world)
+        pb.close()
+        del pb
+    # per-instance error against FP64
     t0 = time.perf_counter()
     laue_err = _fp64_row_checks([W[i] for i in li], [b.outputs[i] for i in li])
     bragg_err, bragg_res = [], []
@@ -542,10 +574,16 @@ def batched_leg(args, world):
     return {
         "instances": len(W), "laue": len(li), "bragg": len(bi),
         "ms_per_batch": ms, "instances_per_s": world * len(W) / sec,
-        "laue_voxel_steps_per_s": world * laue_vs / sec,
         "laue_voxel_steps": laue_vs,
-        "bragg_solves_per_s": world * bragg_solves / sec,
-        "bragg_systems": bragg_sys,
+        "bragg_solves": bragg_solves, "bragg_systems": bragg_sys,
+        "laue_part_alone": {
+            "ms": part_ms.get("laue"),
+            "voxel_steps_per_s": world * laue_vs / (part_ms["laue"] * 1e-3)
+            if "laue" in part_ms else None},
+        "bragg_part_alone": {
+            "ms": part_ms.get("bragg"),
+            "solves_per_s": world * bragg_solves / (part_ms["bragg"] * 1e-3)
+            if "bragg" in part_ms else None},
         "form": "one CUDA graph per replay: per-instance set-up, one "
                 "persistent Laue march launch (compensated FP32, segment sum "
                 "and 2 pi reduction in double, e^{iH} of each row evaluated "
@@ -568,6 +606,99 @@ def batched_leg(args, world):
                    "fp32_single_calls_ms": single32_ms,
                    "fp64_single_calls_ms": single64_ms,
                    "timing": "host wall clock, synchronised"},
+    }
+
+
+def learned_leg(args, world):
+    """Learned shooting guess (Bragg, t 10-100 um, dx 0.25 um, 256 planes x
+    256 px field, 1-32 segments within 5 um of the surface, 64 s over +-5
+    Darwin widths; thickness up to ``--learned-tmax``).  Training data:
+    the plain solves (zero start, mixed precision, true residual 1e-6, ample
+    for a starting guess) of ``--learned-train`` instances, 64 samples each; the U-Net is trained on the GPU by the library's kernels.
+    On ``--learned-test`` held-out instances every system is solved to true
+    residual 1e-8 from the zero start (plain), the perfect-crystal start and
+    the learned start (network inference included in its time), in the
+    mixed-precision form, and from the zero start in plain FP64."""
+    import torch
+    from dyfox_gb300 import learned as Lm
+    from dyfox_gb300.workloads import learned_guess_instances
+    inst = learned_guess_instances(args.learned_train + args.learned_test,
+                                   t_range=(10e-6, args.learned_tmax))
+    train, test = inst[:args.learned_train], inst[args.learned_train:]
+    t0 = time.perf_counter()
+    Xs, Ts, it_train = [], [], []
+    for w in train:
+        X, h0, v0 = Lm.instance_inputs(w)
+        v, info, _ = Lm.solve_instance(w, tol=1e-6)
+        Xs.append(X)
+        Ts.append(Lm.targets(v, h0, v0, w["col0"], w["field"]))
+        it_train.append(float(info[:, 1].float().mean()))
+        del v, info
+    X = torch.cat(Xs)
+    T = torch.cat(Ts)
+    del Xs, Ts
+    data_s = time.perf_counter() - t0
+    net = Lm.UNet(batch=8, H=256, W=256, seed=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = net.train(X, T, epochs=args.learned_epochs, lr=1e-3,
+                     decay_every=max(1, args.learned_epochs // 2))
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    n_samples = X.shape[0]
+    del X, T
+    rows = []
+    for w in test:
+        Xt, h0, v0 = Lm.instance_inputs(w)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        y = net.predict(Xt)
+        x0 = Lm.initial_guess(w, v0, y)
+        b.record()
+        torch.cuda.synchronize()
+        infer_ms = a.elapsed_time(b)
+        row = {"Nz": w["cfg"].Nz, "Nx": w["cfg"].Nx, "segments": len(w["segs"]),
+               "inference_ms": infer_ms}
+        for name, start, prec in (("zero", None, "fp32"),
+                                  ("pristine", Lm.initial_guess(w, v0), "fp32"),
+                                  ("learned", x0, "fp32"),
+                                  ("zero_fp64", None, "fp64")):
+            v, info, ms = Lm.solve_instance(w, x0=start, tol=1e-8,
+                                            precision=prec)
+            inf = info.cpu().numpy()
+            row[name] = {"ms": ms + (infer_ms if name == "learned" else 0.0),
+                         "iterations_mean": float(inf[:, 1].mean()),
+                         "iterations_max": int(inf[:, 1].max()),
+                         "max_true_residual": float(inf[:, 0].max()),
+                         "converged": bool((inf[:, 2] == 0).all())}
+            del v, info
+        rows.append(row)
+    def tot(key, f):
+        return sum(r[key][f] for r in rows)
+    n_solves = sum(len(w["s"]) for w in test)
+    return {
+        "train_instances": len(train), "train_samples": n_samples,
+        "test_instances": len(test), "test_solves": n_solves,
+        "planes": len(train[0]["ys"]) if train else None,
+        "field_px": train[0]["field"] if train else None,
+        "data_generation_s": data_s, "training_s": train_s,
+        "epochs": args.learned_epochs, "loss_first_epoch": hist[0],
+        "loss_last_epoch": hist[-1],
+        "train_iterations_mean": float(np.mean(it_train)),
+        "per_instance": rows,
+        "iterations_mean": {k: tot(k, "iterations_mean") / len(rows)
+                            for k in ("zero", "pristine", "learned",
+                                      "zero_fp64")},
+        "bragg_solves_per_s": {k: world * n_solves / (tot(k, "ms") * 1e-3)
+                               for k in ("zero", "pristine", "learned",
+                                         "zero_fp64")},
+        "form": "learned start: mixed-precision solve from v0 + U-Net "
+                "prediction, inference included; zero_fp64: plain FP64 "
+                "from the zero start (the repo's start); tolerance 1e-8",
+        "reading": "the configuration trains on 20k solves; this leg "
+                   "trains on --learned-train x 64 so the default bench "
+                   "stays within minutes",
     }
 
 

@@ -19,7 +19,10 @@
 // at true relative residual <= tol computed in double; a restart cycle
 // stops its inner iteration once the estimated residual has dropped by
 // kMixedInnerDrop, below which the single-precision operator's own error
-// makes further inner steps useless.
+// makes further inner steps useless.  Where single precision is not
+// accurate enough for a system (thick slabs, long marches), a restart cycle
+// that does not halve the true residual switches that system's Arnoldi
+// products to double for the rest of its solve.
 #include <math.h>
 #include <string.h>
 
@@ -230,9 +233,12 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
         else bragg_march<CPL>(cb, ch, e0, ieg, a.Nz, Nx, a.inc, nullptr, A0,
                               A1, W);
     };
-    // The Arnoldi operator: W <- M A src, in single precision when MIXED.
+    // Single-precision Arnoldi products (MIXED, until a cycle shows that
+    // they no longer lower the true residual).
+    bool use32 = MIXED;
+    // The Arnoldi operator: W <- M A src, in single precision when use32.
     auto inner_op = [&](const double2 *src) {
-        if (MIXED) {
+        if (MIXED && use32) {
             bragg_march32<CPL>(cb32, ch32, e0f, iegf, a.Nz, Nx, nullptr, src,
                                reinterpret_cast<float2 *>(A0),
                                reinterpret_cast<float2 *>(A1), W);
@@ -241,7 +247,7 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
         }
     };
     auto precond = [&]() {
-        if (MIXED)
+        if (MIXED && use32)
             precond_apply32(W, reinterpret_cast<float2 *>(A0),
                             reinterpret_cast<float2 *>(A1), a.plan, a.tw32,
                             iT32);
@@ -296,7 +302,8 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
                 const double tmp = norm2(W);
                 // inner stopping level of this cycle
                 const double pstop =
-                    MIXED ? fmax(ptol, kMixedInnerDrop * tmp) : ptol;
+                    MIXED && use32 ? fmax(ptol, kMixedInnerDrop * tmp) : ptol;
+                const double rprev = rnorm;
                 for (int x = tid; x < Nx; x += nt) V[x] = cscale(1.0 / tmp, W[x]);
                 for (int j = tid; j <= m; j += nt)
                     S[j] = make_double2(j == 0 ? tmp : 0.0, 0.0);
@@ -407,7 +414,9 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
                 __syncthreads();
                 rnorm = norm2(W);
                 if (rnorm <= atol) { code = 0; break; }
-                if (breakdown) break;
+                if (MIXED && use32 && rnorm > 0.5 * rprev)
+                    use32 = false;
+                else if (breakdown) break;
                 if (presid <= ptol)
                     ptol_max_factor = fmax(eps, 0.25 * ptol_max_factor);
                 else

@@ -565,8 +565,9 @@ __global__ void he_init_kernel(float *p, long n, float stdev,
 }
 
 // Network input from the top depth slices of H: x[n][y][x][2k, 2k+1] =
-// cos, sin H(plane y, slice k, column col0 + x) for k < 8; x[..][16] = s_n;
-// channels 17..31 zero.  h: (n_y, 8, Nx) doubles.
+// cos, sin H(plane y, slice k, column (col0 + x) mod Nx) for k < 8 (the
+// lateral grid is periodic); x[..][16] = s_n; channels 17..31 zero.
+// h: (n_y, 8, Nx) doubles.
 __global__ void features_kernel(const double *h, int n_y, int Nx, int col0,
                                 int W, const double *s, int n_s, bf16 *out) {
     const long total = (long)n_s * n_y * W;
@@ -578,7 +579,7 @@ __global__ void features_kernel(const double *h, int n_y, int Nx, int col0,
         const int n = (int)(t / n_y);
         bf16 *o = out + (size_t)i * kUnetCin;
         for (int k = 0; k < 8; ++k) {
-            const double hv = h[((size_t)y * 8 + k) * Nx + col0 + x];
+            const double hv = h[((size_t)y * 8 + k) * Nx + (col0 + x) % Nx];
             double sn, c;
             sincos(hv, &sn, &c);
             o[2 * k] = __float2bfloat16_rn((float)c);
@@ -1042,7 +1043,7 @@ extern "C" int dyfox_unet_features(const double *h_top, int n_y, int Nx,
                                    int n_s, void *x_out, void *stream) {
     set_error("");
     if (!h_top || !s_values || !x_out || n_y < 1 || n_s < 1 || W < 1 ||
-        col0 < 0 || col0 + W > Nx) {
+        Nx < 1 || col0 < 0 || col0 >= Nx) {
         set_error("bad feature arguments (n_y=%d Nx=%d col0=%d W=%d n_s=%d)",
                   n_y, Nx, col0, W, n_s);
         return DYFOX_EINVAL;

@@ -307,22 +307,34 @@ def pristine_v(s_values, cfg, xtal):
     return out
 
 
-def instance_inputs(inst):
-    """(features (n_s, n_y, field, 32) bf16, H at z = 0 (n_y, Nx) float64,
-    v0 (n_s,) complex) of a learned-guess instance."""
+def full_width(Nx):
+    """Network width covering a periodic lateral grid of Nx columns."""
+    return -(-int(Nx) // 8) * 8
+
+
+def instance_h(inst):
+    """H on the first 8 depth slices of every plane, (n_y, 8, Nx)."""
     torch = _lib.torch_cuda()
     from .dislocations import H_rows
     cfg, x = inst["cfg"], inst["xtal"]
     ys = np.asarray(inst["ys"], float)
     if inst["segs"]:
-        h = H_rows(inst["segs"], cfg.Nx, N_SLICES, cfg.dx, cfg.dz, inst["g"],
-                   x.nu, x.a_core, ys)
-    else:
-        h = torch.zeros((len(ys), N_SLICES, cfg.Nx), dtype=torch.float64,
-                        device="cuda")
-    X = features(h, inst["col0"], inst["field"],
-                 np.asarray(inst["s"], float) / s_scale(x))
-    return X, h[:, 0, :].contiguous(), pristine_v(inst["s"], cfg, x)
+        return H_rows(inst["segs"], cfg.Nx, N_SLICES, cfg.dx, cfg.dz,
+                      inst["g"], x.nu, x.a_core, ys)
+    return torch.zeros((len(ys), N_SLICES, cfg.Nx), dtype=torch.float64,
+                       device="cuda")
+
+
+def instance_inputs(inst, col0=None, width=None, h=None):
+    """(features (n_s, n_y, width, 32) bf16 of columns col0 .. col0 +
+    width (mod Nx), H at z = 0 (n_y, Nx) float64, v0 (n_s,) complex) of a
+    learned-guess instance; the field of interest by default."""
+    x = inst["xtal"]
+    h = instance_h(inst) if h is None else h
+    col0 = inst["col0"] if col0 is None else col0
+    width = inst["field"] if width is None else width
+    X = features(h, col0, width, np.asarray(inst["s"], float) / s_scale(x))
+    return X, h[:, 0, :].contiguous(), pristine_v(inst["s"], inst["cfg"], x)
 
 
 def solve_instance(inst, x0=None, tol=1e-8, precision="fp32", restart=40,
@@ -346,24 +358,50 @@ def solve_instance(inst, x0=None, tol=1e-8, precision="fp32", restart=40,
 
 def targets(v, h0, v0, col0, field):
     """Training target of an instance: v (phase-restored solution times
-    e^{+iH(0)}) minus v0 over the field, as (n_s, n_y, field, 2) float32."""
+    e^{+iH(0)}) minus v0 over columns col0 .. col0 + field (mod Nx), as
+    (n_s, n_y, field, 2) float32."""
     torch = _lib.torch_cuda()
     vv = v * torch.exp(1j * h0)[None]
-    d = vv[:, :, col0:col0 + field] - torch.as_tensor(v0, device="cuda")[
+    Nx = vv.shape[-1]
+    cols = torch.arange(col0, col0 + field, device="cuda") % Nx
+    d = vv.index_select(2, cols) - torch.as_tensor(v0, device="cuda")[
         :, None, None]
     return torch.view_as_real(d.to(torch.complex64)).contiguous()
 
 
-def initial_guess(inst, v0, y=None):
+def initial_guess(inst, v0, y=None, col0=None):
     """x0 of the solve: v0(s) on every column of every plane, plus the
-    network's prediction y (n_s, n_y, field, 2) over the field."""
+    network's prediction y (n_s, n_y, width, 2) on columns col0 .. col0 +
+    width (mod Nx; the field of interest by default).  A prediction of
+    the full width (col0 = 0, width >= Nx) covers every column."""
     torch = _lib.torch_cuda()
     cfg = inst["cfg"]
     n_s, n_y = len(inst["s"]), len(inst["ys"])
     x0 = torch.as_tensor(v0, dtype=torch.complex128, device="cuda")[
         :, None, None].expand(n_s, n_y, cfg.Nx).clone()
     if y is not None:
-        c0, f = inst["col0"], inst["field"]
-        x0[:, :, c0:c0 + f] += torch.view_as_complex(
-            y.contiguous()).to(torch.complex128)
+        c0 = inst["col0"] if col0 is None else col0
+        width = min(int(y.shape[2]), cfg.Nx)
+        cols = torch.arange(c0, c0 + width, device="cuda") % cfg.Nx
+        x0.index_add_(2, cols, torch.view_as_complex(
+            y[:, :, :width].contiguous()).to(torch.complex128))
     return x0.contiguous()
+
+
+def predict_full(net, inst, h=None, batch=None):
+    """The network applied to the whole periodic lateral grid of an
+    instance (a fully convolutional network trained on windows):
+    (n_s, n_y, full_width(Nx), 2) float32.  ``net`` supplies the trained
+    parameters; a network of the full width shares them."""
+    cfg = inst["cfg"]
+    W = full_width(cfg.Nx)
+    key = (len(inst["ys"]), W)
+    cache = getattr(net, "_full", {})
+    wide = cache.get(key)
+    if wide is None:
+        wide = UNet(batch=batch or net.batch, H=len(inst["ys"]), W=W)
+        cache[key] = wide
+        net._full = cache
+    wide.load(net.params)
+    X, _, _ = instance_inputs(inst, col0=0, width=W, h=h)
+    return wide.predict(X)

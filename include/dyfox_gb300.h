@@ -315,8 +315,9 @@ int dyfox_unet_backward(dyfox_unet *net, const float *target, float *loss,
 int dyfox_unet_adam(dyfox_unet *net, float lr, float beta1, float beta2,
                     float eps, void *stream);
 /* Network input from the top 8 depth slices of H: h_top (n_y, 8, Nx)
- * doubles, columns [col0, col0 + W), s_values (n_s doubles, already
- * scaled); x_out (n_s, n_y, W, 32) bfloat16. */
+ * doubles, columns (col0 + x) mod Nx for x < W (the lateral grid is
+ * periodic), s_values (n_s doubles, already scaled); x_out (n_s, n_y, W,
+ * 32) bfloat16. */
 int dyfox_unet_features(const double *h_top, int n_y, int Nx, int col0,
                         int W, const double *s_values, int n_s, void *x_out,
                         void *stream);

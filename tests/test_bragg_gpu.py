@@ -256,15 +256,16 @@ def test_mixed_config1_planes(gpu, diamond400):
     assert rel_l2(np_(o32), np_(o64)) < 1e-8
 
 
-@pytest.mark.parametrize("t,dx", [(20e-6, 0.25e-6), (40e-6, 0.125e-6)])
-def test_wide_lateral_grids(gpu, diamond400, t, dx):
+@pytest.mark.parametrize("t,dx,half", [(20e-6, 0.25e-6, 2e-6),
+                                       (10e-6, 0.125e-6, 150e-6)])
+def test_wide_lateral_grids(gpu, diamond400, t, dx, half):
     """Nx above 512 (256-thread systems, 4 and 16 columns a thread; Nx 776
-    and 2928): FP64 and mixed solves converge and agree."""
+    and 3148): FP64 and mixed solves converge and agree."""
     from dyfox_gb300.bragg import solve_scan
     from dyfox_gb300.bragg_geometry import BraggConfig, bragg_g_vector
     from dyfox_gb300.dislocations import burgers_vector, straight_segment
     from dyfox_gb300.units import deviation_from_urad
-    cfg = BraggConfig(diamond400, t_crystal=t, dx=dx, half_x=8 * dx)
+    cfg = BraggConfig(diamond400, t_crystal=t, dx=dx, half_x=half)
     assert cfg.Nx > 512
     b = burgers_vector(np.eye(3), [1, 0, -1], diamond400.b_mag, +1)
     seg = straight_segment(np.array([1.0, 0.0, 1.0]) / np.sqrt(2.0), b,

@@ -57,7 +57,9 @@ def test_single_conv_products(gpu, rng, N, H, W, Cin, Cout):
     y = conv("fwd", X=dev_bf16(X), Wk=dev_bf16(Wt), bias=torch.tensor(b).cuda(),
              Cout=Cout).float().cpu().numpy()
     ref = np.maximum(U.conv3(X, Wt, b.astype(np.float64)), 0.0)
-    assert np.all(np.abs(y - ref) <= 2.0 ** -7 * np.abs(ref) + 1e-30)
+    # one unit in the last place, or FP32 accumulation error where the
+    # output is within it of zero (the ReLU then clamps either way)
+    assert np.all(np.abs(y - ref) <= 2.0 ** -7 * np.abs(ref) + 1e-5)
     assert np.mean(y != U.bf16(ref)) <= 2e-3
     # data and weight gradients: FP32 accumulation of exact products
     dx_ref, dw_ref, _ = U.conv3_backward(X, Wt, G)
@@ -100,7 +102,7 @@ def test_layerwise_against_the_oracle(gpu, rng):
         Wr = U.bf16(p32[name + ".W"])
         ref = np.maximum(U.conv3(xin, Wr, p32[name + ".b"]), 0.0)
         got = net.buffer("act", i, n).cpu().numpy()
-        assert np.all(np.abs(got - ref) <= 2.0 ** -7 * np.abs(ref) + 1e-30), \
+        assert np.all(np.abs(got - ref) <= 2.0 ** -7 * np.abs(ref) + 1e-5), \
             (name, float(np.abs(got - ref).max()))
         assert np.mean(got != U.bf16(ref)) <= 2e-3, name
     for l in range(3):
@@ -203,6 +205,10 @@ def test_features(gpu, rng):
                                               (2, 5, 24)))
     assert np.array_equal(got[0, ..., 16], np.full((5, 24), U.bf16(0.3)))
     assert np.all(got[..., 17:] == 0)
+    # columns wrap around the periodic lateral grid
+    wrap = features(torch.tensor(h).cuda(), 30, 24, s).float().cpu().numpy()
+    cols = np.arange(30, 54) % 40
+    assert np.array_equal(wrap[0, ..., 0], U.bf16(np.cos(h[:, 0, cols])))
 
 
 def test_bad_shapes(gpu):

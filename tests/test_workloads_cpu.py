@@ -25,5 +25,5 @@ def test_batched_uneven_mix_and_ranges():
         else:
             c = w["cfg"]
             assert 1 <= len(w["ys"]) <= 8
-            assert 5e-6 - c.dz <= c.t_crystal <= 40e-6 + c.dz
+            assert 5e-6 - c.dz <= c.t_crystal <= 20e-6 + c.dz
             assert c.Nx == 2 * (round(c.half_x / c.dx) + 2 * c.Nz + 16)
