@@ -158,7 +158,8 @@ __device__ void bragg_march(const double2 *__restrict__ cb,
 // The same march in single precision, for the inner (Arnoldi) products of
 // the mixed-precision solve: couplings cb, ch and the step factors in float,
 // the inputs rounded to float (NULL means zero), the result widened into
-// out.  ex0, ex1: float2 exchange rows of Nx.
+// out.  ex0, ex1: two float2 exchange rows of Nx each (2 Nx float2); step k
+// writes the half k % 2, so one barrier a step suffices.
 template <int CPL>
 __device__ void bragg_march32(const float2 *__restrict__ cb,
                               const float2 *__restrict__ ch, float2 e0,
@@ -185,6 +186,7 @@ __device__ void bragg_march32(const float2 *__restrict__ cb,
     }
     for (int k = 0; k < Nz - 1; ++k) {
         const float2 *cbk = cb + (size_t)k * Nx, *chk = ch + (size_t)k * Nx;
+        float2 *e0r = ex0 + (k & 1) * Nx, *e1r = ex1 + (k & 1) * Nx;
 #pragma unroll
         for (int i = 0; i < CPL; ++i) {
             const int x = tid + i * nt;
@@ -192,21 +194,23 @@ __device__ void bragg_march32(const float2 *__restrict__ cb,
                 const float2 b = __ldg(cbk + x), h = __ldg(chk + x);
                 const float2 u = cadd(D0[i], cmulz(b, Dg[i]));
                 const float2 v = cmulz(csub(Dg[i], cmulz(h, D0[i])), ieg);
-                ex0[x + 1 == Nx ? 0 : x + 1] = cmulz(e0, u);
-                ex1[x == 0 ? Nx - 1 : x - 1] = v;
+                e0r[x + 1 == Nx ? 0 : x + 1] = cmulz(e0, u);
+                e1r[x == 0 ? Nx - 1 : x - 1] = v;
             }
         }
+        // The rows of step k are complete; those of step k - 1 (the other
+        // half) were read by every thread before it wrote step k.
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < CPL; ++i) {
             const int x = tid + i * nt;
             if (x < Nx) {
-                D0[i] = ex0[x];
-                Dg[i] = ex1[x];
+                D0[i] = e0r[x];
+                Dg[i] = e1r[x];
             }
         }
-        __syncthreads();
     }
+    __syncthreads();
 #pragma unroll
     for (int i = 0; i < CPL; ++i) {
         const int x = tid + i * nt;

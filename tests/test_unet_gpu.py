@@ -27,6 +27,10 @@ from oracle import unet_oracle as U
 pytestmark = pytest.mark.gpu
 
 
+def np_(t):
+    return t.detach().cpu().numpy()
+
+
 def _setup(rng, n=2, H=16, W=16, seed=2):
     p = U.init_params(seed=seed)
     for k in p:
@@ -220,3 +224,47 @@ def test_bad_shapes(gpu):
     with pytest.raises(ValueError):
         net.forward(torch.zeros((2, 16, 16, 32), dtype=torch.bfloat16,
                                 device="cuda"))
+
+
+def test_learned_guess_lowers_the_initial_residual(gpu):
+    """End to end on a small configuration (64 planes x 64 px field, 64
+    deviation parameters, t 10-14 um): train on the plain solves of 8
+    instances (3 lateral windows each), then on a held-out instance the
+    network's full-width guess lowers the initial shooting residual
+    |A x0 + d| / |d| below the zero start's 1, and the solve from it still
+    meets its tolerance."""
+    from dyfox_gb300 import learned as Lm
+    from dyfox_gb300.bragg import apply_operator
+    from dyfox_gb300.workloads import learned_guess_instances
+    torch = gpu
+    inst = learned_guess_instances(9, seed=11, t_range=(10e-6, 14e-6),
+                                   n_planes=64, field=64, n_s=64)
+    Xs, Ts = [], []
+    for w in inst[:8]:
+        h = Lm.instance_h(w)
+        v, info, _ = Lm.solve_instance(w, tol=1e-6)
+        Nx = w["cfg"].Nx
+        for c0 in (w["col0"], (w["col0"] + Nx // 3) % Nx,
+                   (w["col0"] + 2 * Nx // 3) % Nx):
+            X, h0, v0 = Lm.instance_inputs(w, col0=c0, h=h)
+            Xs.append(X)
+            Ts.append(Lm.targets(v, h0, v0, c0, w["field"]))
+    X, T = torch.cat(Xs), torch.cat(Ts)
+    net = Lm.UNet(batch=8, H=64, W=64, seed=2)
+    hist = net.train(X, T, epochs=12, lr=1e-3, decay_every=4)
+    assert hist[-1] < 0.7 * hist[0]
+    w = inst[8]
+    h = Lm.instance_h(w)
+    _, h0, v0 = Lm.instance_inputs(w, h=h)
+    x0 = Lm.initial_guess(w, v0, Lm.predict_full(net, w, h=h), col0=0)
+    inc = torch.ones((len(w["s"]), len(w["ys"]), w["cfg"].Nx),
+                     dtype=torch.complex128, device="cuda")
+    d = apply_operator(w["segs"], w["s"], w["cfg"], w["ys"], w["xtal"],
+                       w["g"], "march", in0=inc)
+    Ax = apply_operator(w["segs"], w["s"], w["cfg"], w["ys"], w["xtal"],
+                        w["g"], "march", in1=x0)
+    r0 = float(torch.linalg.vector_norm(Ax + d) / torch.linalg.vector_norm(d))
+    assert r0 < 0.95
+    _, info, _ = Lm.solve_instance(w, x0=x0, tol=1e-8)
+    info = np_(info) if hasattr(info, "cpu") else info
+    assert info[:, 0].max() < 1e-8 and np.all(info[:, 2] == 0)
