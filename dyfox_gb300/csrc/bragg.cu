@@ -21,8 +21,9 @@
 // kMixedInnerDrop, below which the single-precision operator's own error
 // makes further inner steps useless.  Where single precision is not
 // accurate enough for a system (thick slabs, long marches), a restart cycle
-// that lowers the true residual by less than 10% switches that system's
-// Arnoldi products to double for the rest of its solve.
+// whose inner iteration estimated a reduction of 10x or more while the true
+// residual did not halve switches that system's Arnoldi products to double
+// for the rest of its solve.
 #include <math.h>
 #include <string.h>
 
@@ -414,7 +415,8 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
                 __syncthreads();
                 rnorm = norm2(W);
                 if (rnorm <= atol) { code = 0; break; }
-                if (MIXED && use32 && rnorm > 0.9 * rprev)
+                if (MIXED && use32 && rnorm > 0.5 * rprev &&
+                    presid < 0.1 * tmp)
                     use32 = false;
                 else if (breakdown) break;
                 if (presid <= ptol)

@@ -146,6 +146,23 @@ conv_gemm_kernel(const ConvArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = warp >> 1, wn = warp & 1;
     const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+    // FWD / DGRAD: the tile's 64 output pixels stay fixed over the whole K
+    // loop; their (y, x) are decoded once (y = -2^20 marks a pixel past M).
+    __shared__ int sRowY[kBM], sRowX[kBM];
+    if (MODE != CM_WGRAD) {
+        for (int r = tid; r < kBM; r += kThreads) {
+            const int p = m0 + r;
+            int y = -(1 << 20), x = 0;
+            if (p < a.M) {
+                const int rem = p % (a.H * a.W);
+                y = rem / a.W;
+                x = rem - y * a.W;
+            }
+            sRowY[r] = y;
+            sRowX[r] = x;
+        }
+        __syncthreads();
+    }
     const int kt0 = blockIdx.z * a.ktiles_per_split;
     const int ktiles_total = (a.K + kBK - 1) / kBK;
     int kt1 = kt0 + a.ktiles_per_split;
@@ -159,16 +176,19 @@ conv_gemm_kernel(const ConvArgs a) {
             const int t = k0 / C, c0 = k0 - t * C;
             const int dy = t / 3 - 1, dx = t % 3 - 1;
             const bf16 *src = MODE == CM_FWD ? a.X : a.G;
-            // A: 64 pixels x 4 chunks
+            // A: 64 pixels x 4 chunks; the source pixel is p + (dy, dx)
+            // (forward) or p - (dy, dx) (data gradient).
+            const int sy = MODE == CM_FWD ? dy : -dy;
+            const int sx = MODE == CM_FWD ? dx : -dx;
+            const int sq = sy * W + sx;
             for (int c = tid; c < kBM * 4; c += kThreads) {
                 const int row = c >> 2, kc = c & 3;
-                const int p = m0 + row;
-                int q = -1;
-                if (p < a.M)
-                    q = MODE == CM_FWD ? shifted_pixel(p, H, W, dy, dx)
-                                       : shifted_pixel(p, H, W, -dy, -dx);
-                const bf16 *g = q >= 0 ? src + (size_t)q * C + c0 + 8 * kc : src;
-                cp_async16_zfill(&sA[stage][row * kKStride + 8 * kc], g, q >= 0);
+                const int y = sRowY[row] + sy, x = sRowX[row] + sx;
+                const bool ok = (unsigned)y < (unsigned)H &&
+                                (unsigned)x < (unsigned)W;
+                const bf16 *g = ok ? src + (size_t)(m0 + row + sq) * C + c0 + 8 * kc
+                                   : src;
+                cp_async16_zfill(&sA[stage][row * kKStride + 8 * kc], g, ok);
             }
             // B: BN output channels x 4 chunks, rows of Wk[n][t][c]
             for (int c = tid; c < BN * 4; c += kThreads) {
