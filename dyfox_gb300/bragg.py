@@ -73,7 +73,11 @@ def _L():
     return L
 
 
-def _desc(cfg, xtal, n_y, n_s, n_seg, tol, restart, maxiter, prec=FP64):
+FORCE_RESUME = 1
+
+
+def _desc(cfg, xtal, n_y, n_s, n_seg, tol, restart, maxiter, prec=FP64,
+          flags=0):
     d = BraggDesc()
     for name in ("sig0", "sig_h", "sig_hbar"):
         v = complex(getattr(xtal, name))
@@ -89,6 +93,7 @@ def _desc(cfg, xtal, n_y, n_s, n_seg, tol, restart, maxiter, prec=FP64):
     d.beam_centre = float(getattr(cfg, "beam_centre", 0.0))
     d.tol, d.restart, d.maxiter = float(tol), int(restart), int(maxiter)
     d.precision = as_precision(prec).code
+    d.flags = int(flags)
     return d
 
 
@@ -96,9 +101,10 @@ class _Problem:
     """Device-side inputs of one call: segment table, planes, s values."""
 
     def __init__(self, seg_list, s_values, cfg, y_values, xtal, g_vec,
-                 precision=FP64):
+                 precision=FP64, flags=0):
         torch = _lib.torch_cuda()
         self.prec = as_precision(precision)
+        self.flags = flags
         self.torch = torch
         self.cfg, self.xtal = cfg, xtal
         self.seg_list, self.g_vec = seg_list or [], g_vec
@@ -116,7 +122,7 @@ class _Problem:
     def desc(self, tol=1e-10, restart=40, maxiter=25, n_s=None):
         return _desc(self.cfg, self.xtal, len(self.y),
                      len(self.s) if n_s is None else n_s, self.n_seg, tol,
-                     restart, maxiter, self.prec)
+                     restart, maxiter, self.prec, self.flags)
 
     def workspace(self, d):
         n = _L().dyfox_bragg_workspace_bytes(d)
@@ -130,7 +136,8 @@ def _yp(prob):
 
 
 def solve_scan(seg_list, s_values, cfg, y_values, xtal, g_vec, tol=1e-10,
-               restart=40, maxiter=25, x0=None, *, precision=FP64):
+               restart=40, maxiter=25, x0=None, *, precision=FP64,
+               _flags=0):
     """All deviation parameters x all planes in one launch.
 
     Returns (out, info): out is a (n_s, n_y, Nx) complex128 CUDA tensor of
@@ -138,7 +145,7 @@ def solve_scan(seg_list, s_values, cfg, y_values, xtal, g_vec, tol=1e-10,
     residual, inner iterations, code, |b|) per system.
     """
     prob = _Problem(seg_list, s_values, cfg, y_values, xtal, g_vec,
-                    precision)
+                    precision, _flags)
     return _run(prob, tol, restart, maxiter, x0)
 
 

@@ -22,8 +22,9 @@
 // makes further inner steps useless.  Where single precision is not
 // accurate enough for a system (thick slabs, long marches), a restart cycle
 // whose inner iteration estimated a reduction of 10x or more while the true
-// residual did not halve switches that system's Arnoldi products to double
-// for the rest of its solve.
+// residual did not halve ends the mixed solve, and the CTA finishes that
+// system in double from the solution reached (each path compiled on its
+// own, so the single-precision loop carries no double-precision branch).
 #include <math.h>
 #include <string.h>
 
@@ -190,9 +191,16 @@ constexpr double kMixedInnerDrop = 1e-5;
 
 // The solve of system `sys` (deviation parameter sys / n_y, plane
 // sys % n_y) of `a` by the calling CTA.  smem: gmres_smem(Nx, restart).
+// warm: start from the X already in place (else from a.use_x0's rule);
+// inner0: inner iterations already spent on this system.  Returns -1 when
+// the solve ended (result and info written); a MIXED solve whose single-
+// precision products stopped lowering the true residual returns its inner
+// iteration count instead and writes nothing, and the caller continues in
+// double from the X reached so far.
 template <int CPL, bool MIXED>
-__device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
-                                             unsigned char *smem) {
+__device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
+                                            unsigned char *smem, bool warm,
+                                            int inner0) {
     const int Nx = a.Nx, m = a.restart;
     double2 *A0 = reinterpret_cast<double2 *>(smem);
     double2 *A1 = A0 + Nx;
@@ -234,12 +242,9 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
         else bragg_march<CPL>(cb, ch, e0, ieg, a.Nz, Nx, a.inc, nullptr, A0,
                               A1, W);
     };
-    // Single-precision Arnoldi products (MIXED, until a cycle shows that
-    // they no longer lower the true residual).
-    bool use32 = MIXED;
-    // The Arnoldi operator: W <- M A src, in single precision when use32.
+    // The Arnoldi operator: W <- M A src, in single precision when MIXED.
     auto inner_op = [&](const double2 *src) {
-        if (MIXED && use32) {
+        if (MIXED) {
             bragg_march32<CPL>(cb32, ch32, e0f, iegf, a.Nz, Nx, nullptr, src,
                                reinterpret_cast<float2 *>(A0),
                                reinterpret_cast<float2 *>(A1), W);
@@ -248,7 +253,7 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
         }
     };
     auto precond = [&]() {
-        if (MIXED && use32)
+        if (MIXED)
             precond_apply32(W, reinterpret_cast<float2 *>(A0),
                             reinterpret_cast<float2 *>(A1), a.plan, a.tw32,
                             iT32);
@@ -260,7 +265,7 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
     matvec(nullptr);
     for (int x = tid; x < Nx; x += nt) {
         B[x] = make_double2(-W[x].x, -W[x].y);
-        if (!a.use_x0) X[x] = make_double2(0.0, 0.0);
+        if (!a.use_x0 && !warm) X[x] = make_double2(0.0, 0.0);
     }
     __syncthreads();
     const double bnrm2 = norm2(B);
@@ -280,7 +285,7 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
         double presid = 0.0;
         // r = b - A x0 (b when x0 is zero)
         bool nonzero = false;
-        if (a.use_x0) {
+        if (a.use_x0 || warm) {
             double2 t = make_double2(0.0, 0.0);
             for (int x = tid; x < Nx; x += nt) t.x += cabs2(X[x]);
             nonzero = block_sum(t, red).x > 0.0;
@@ -303,7 +308,7 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
                 const double tmp = norm2(W);
                 // inner stopping level of this cycle
                 const double pstop =
-                    MIXED && use32 ? fmax(ptol, kMixedInnerDrop * tmp) : ptol;
+                    MIXED ? fmax(ptol, kMixedInnerDrop * tmp) : ptol;
                 const double rprev = rnorm;
                 for (int x = tid; x < Nx; x += nt) V[x] = cscale(1.0 / tmp, W[x]);
                 for (int j = tid; j <= m; j += nt)
@@ -415,10 +420,10 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
                 __syncthreads();
                 rnorm = norm2(W);
                 if (rnorm <= atol) { code = 0; break; }
-                if (MIXED && use32 && rnorm > 0.5 * rprev &&
-                    presid < 0.1 * tmp)
-                    use32 = false;
-                else if (breakdown) break;
+                if (MIXED && ((rnorm > 0.5 * rprev && presid < 0.1 * tmp) ||
+                              a.force_resume))
+                    return inner0 + inner;        // single precision stalled
+                if (breakdown) break;
                 if (presid <= ptol)
                     ptol_max_factor = fmax(eps, 0.25 * ptol_max_factor);
                 else
@@ -434,18 +439,59 @@ __device__ __forceinline__ void gmres_system(const BraggArgs &a, int sys,
     for (int x = tid; x < Nx; x += nt) out[x] = cmulz(X[x], __ldg(e0h + x));
     if (tid == 0) {
         info[0] = bnrm2 > 0.0 ? rnorm / bnrm2 : 0.0;
-        info[1] = inner;
+        info[1] = inner0 + inner;
         info[2] = code;
         info[3] = bnrm2;
     }
     (void)flags;
+    return -1;
 }
 
-// One CTA per system of one solve call.
+// A system in the requested precision.  A mixed solve that stalls leaves
+// its solution so far in X and marks the system (code -1, iterations spent
+// in info[1]) for bragg_resume_kernel, which finishes it in double; the
+// double path is a separate launch so that the single-precision kernel
+// carries none of it.
 template <int CPL, bool MIXED>
-__global__ void bragg_gmres_kernel(const BraggArgs a) {
+__device__ __forceinline__ void solve_system(const BraggArgs &a, int sys,
+                                             unsigned char *smem) {
+    const int spent = gmres_system<CPL, MIXED>(a, sys, smem, false, 0);
+    if (MIXED && spent >= 0 && threadIdx.x == 0) {
+        double *info = a.info + (size_t)sys * 4;
+        info[1] = spent;
+        info[2] = -1.0;
+    }
+}
+
+// Continuation in double of the systems a mixed solve marked.
+template <int CPL>
+__device__ __forceinline__ void resume_system(const BraggArgs &a, int sys,
+                                              unsigned char *smem) {
+    const double *info = a.info + (size_t)sys * 4;
+    if (info[2] != -1.0) return;          // uniform over the CTA
+    gmres_system<CPL, false>(a, sys, smem, true, (int)info[1]);
+}
+
+// The GMRES kernels are compiled for their CTA size only: holding the
+// 128-thread kernel to 5 resident CTAs an SM (96 registers) was measured
+// 18% slower on config 1 than letting it take the registers it needs.
+constexpr int gmres_min_blocks(int) { return 1; }
+
+// One CTA of NT threads per system of one solve call.
+template <int CPL, bool MIXED, int NT>
+__global__ void __launch_bounds__(NT, gmres_min_blocks(NT))
+bragg_gmres_kernel(const BraggArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    gmres_system<CPL, MIXED>(a, blockIdx.x, smem);
+    solve_system<CPL, MIXED>(a, blockIdx.x, smem);
+}
+
+// After a mixed launch: one CTA per system, returning at once unless the
+// system was marked.
+template <int CPL, int NT>
+__global__ void __launch_bounds__(NT, gmres_min_blocks(NT))
+bragg_resume_kernel(const BraggArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    resume_system<CPL>(a, blockIdx.x, smem);
 }
 
 // Matvec / preconditioner for parity checks: one CTA per system.
@@ -537,6 +583,10 @@ static int bragg_validate(const dyfox_bragg_desc *d) {
                   d->precision);
         return DYFOX_EINVAL;
     }
+    if (d->flags & ~DYFOX_BRAGG_FORCE_RESUME) {
+        set_error("unknown Bragg flags 0x%x", d->flags);
+        return DYFOX_EINVAL;
+    }
     return DYFOX_OK;
 }
 
@@ -625,6 +675,7 @@ static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
     a->tol = d->tol;
     a->restart = d->restart;
     a->maxiter = d->maxiter;
+    a->force_resume = (d->flags & DYFOX_BRAGG_FORCE_RESUME) ? 1 : 0;
     cudaError_t e;
     const double *y = y_src;
     if (!y_on_device) {
@@ -665,16 +716,54 @@ static cudaError_t resident(K *k, int threads, size_t smem) {
     return occ >= 1 ? cudaSuccess : cudaErrorLaunchOutOfResources;
 }
 
+// The kernel of CPL columns a thread for `threads` (128 or 256) threads:
+// CPL 1, 2 only occur with 128 threads, 8 and 16 only with 256.
+template <int CPL, bool MIXED>
+static void (*gmres_kernel_for(int threads))(const BraggArgs) {
+    if constexpr (CPL <= 2) {
+        return bragg_gmres_kernel<CPL, MIXED, 128>;
+    } else if constexpr (CPL >= 8) {
+        return bragg_gmres_kernel<CPL, MIXED, 256>;
+    } else {
+        return threads == 128 ? bragg_gmres_kernel<CPL, MIXED, 128>
+                              : bragg_gmres_kernel<CPL, MIXED, 256>;
+    }
+}
+
+template <int CPL>
+static void (*resume_kernel_for(int threads))(const BraggArgs) {
+    if constexpr (CPL <= 2) {
+        return bragg_resume_kernel<CPL, 128>;
+    } else if constexpr (CPL >= 8) {
+        return bragg_resume_kernel<CPL, 256>;
+    } else {
+        return threads == 128 ? bragg_resume_kernel<CPL, 128>
+                              : bragg_resume_kernel<CPL, 256>;
+    }
+}
+
 template <int CPL, bool MIXED>
 static cudaError_t launch_gmres(const BraggArgs &a, int threads, size_t smem,
                                 int grid, cudaStream_t stream) {
-    auto *k = bragg_gmres_kernel<CPL, MIXED>;
+    auto *k = gmres_kernel_for<CPL, MIXED>(threads);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e) return e;
     }
     if (cudaError_t e = resident(k, threads, smem)) return e;
+    if (MIXED) {
+        auto *r = resume_kernel_for<CPL>(threads);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(
+                r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e) return e;
+        }
+        k<<<grid, threads, smem, stream>>>(a);
+        r<<<grid, threads, smem, stream>>>(a);
+        count_launch(2);
+        return cudaGetLastError();
+    }
     k<<<grid, threads, smem, stream>>>(a);
     count_launch(1);
     return cudaGetLastError();
@@ -700,15 +789,54 @@ static cudaError_t launch_apply(const BraggArgs &a, int threads, size_t smem,
 // ---------------------------------------------------------------------------
 // Pieces used by the batched launcher (batch.cu): one CTA per system of
 // many instances, the instances' arguments in a device array.
-template <int CPL, bool MIXED>
-__global__ void bragg_batch_kernel(const BraggArgs *__restrict__ insts,
-                                   const int2 *__restrict__ systems) {
+template <int CPL, int NT>
+__global__ void __launch_bounds__(NT, gmres_min_blocks(NT))
+bragg_batch_resume_kernel(const BraggArgs *__restrict__ insts,
+                          const int2 *__restrict__ systems) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ BraggArgs a;
     const int2 w = systems[blockIdx.x];
     if (threadIdx.x == 0) a = insts[w.x];
     __syncthreads();
-    gmres_system<CPL, MIXED>(a, w.y, smem);
+    resume_system<CPL>(a, w.y, smem);
+}
+
+template <int CPL, bool MIXED, int NT>
+__global__ void __launch_bounds__(NT, gmres_min_blocks(NT))
+bragg_batch_kernel(const BraggArgs *__restrict__ insts,
+                   const int2 *__restrict__ systems) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ BraggArgs a;
+    const int2 w = systems[blockIdx.x];
+    if (threadIdx.x == 0) a = insts[w.x];
+    __syncthreads();
+    solve_system<CPL, MIXED>(a, w.y, smem);
+}
+
+template <int CPL, bool MIXED>
+static void (*batch_kernel_for(int threads))(const BraggArgs *,
+                                             const int2 *) {
+    if constexpr (CPL <= 2) {
+        return bragg_batch_kernel<CPL, MIXED, 128>;
+    } else if constexpr (CPL >= 8) {
+        return bragg_batch_kernel<CPL, MIXED, 256>;
+    } else {
+        return threads == 128 ? bragg_batch_kernel<CPL, MIXED, 128>
+                              : bragg_batch_kernel<CPL, MIXED, 256>;
+    }
+}
+
+template <int CPL>
+static void (*batch_resume_for(int threads))(const BraggArgs *,
+                                             const int2 *) {
+    if constexpr (CPL <= 2) {
+        return bragg_batch_resume_kernel<CPL, 128>;
+    } else if constexpr (CPL >= 8) {
+        return bragg_batch_resume_kernel<CPL, 256>;
+    } else {
+        return threads == 128 ? bragg_batch_resume_kernel<CPL, 128>
+                              : bragg_batch_resume_kernel<CPL, 256>;
+    }
 }
 
 template <int CPL, bool MIXED>
@@ -716,18 +844,29 @@ static cudaError_t launch_bragg_batch_t(const BraggArgs *insts,
                                         const int2 *systems, int n_sys,
                                         int threads, size_t smem,
                                         cudaStream_t stream) {
-    bragg_batch_kernel<CPL, MIXED><<<n_sys, threads, smem, stream>>>(insts,
-                                                                   systems);
+    batch_kernel_for<CPL, MIXED>(threads)<<<n_sys, threads, smem, stream>>>(
+        insts, systems);
     count_launch(1);
+    if (MIXED) {
+        batch_resume_for<CPL>(threads)<<<n_sys, threads, smem, stream>>>(
+            insts, systems);
+        count_launch(1);
+    }
     return cudaGetLastError();
 }
 
 template <int CPL, bool MIXED>
 static cudaError_t set_smem_t(size_t smem, int threads) {
+    auto *k = batch_kernel_for<CPL, MIXED>(threads);
     cudaError_t e = cudaFuncSetAttribute(
-        bragg_batch_kernel<CPL, MIXED>,
-        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    return e ? e : resident(bragg_batch_kernel<CPL, MIXED>, threads, smem);
+        k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!e) e = resident(k, threads, smem);
+    if (!e && MIXED) {
+        auto *r = batch_resume_for<CPL>(threads);
+        e = cudaFuncSetAttribute(
+            r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    return e;
 }
 
 // Dynamic shared memory of the batch kernel, and a check that one CTA fits

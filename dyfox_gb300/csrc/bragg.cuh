@@ -368,6 +368,7 @@ struct BraggArgs {
     double *info;                 // (n_sys, 4)
     double tol;
     int restart, maxiter, use_x0;
+    int force_resume;             // DYFOX_BRAGG_FORCE_RESUME (checks)
 };
 
 }  // namespace dyfox

@@ -164,8 +164,14 @@ typedef struct dyfox_bragg_desc {
     double tol;                              /* GMRES rtol (true residual) */
     int restart, maxiter;                    /* GMRES restart, maxiter     */
     int precision;                           /* DYFOX_FP64 / DYFOX_FP32    */
-    unsigned flags;                          /* reserved, 0                */
+    unsigned flags;                          /* DYFOX_BRAGG_* or 0         */
 } dyfox_bragg_desc;
+
+/* dyfox_bragg_desc.flags: for checks, a DYFOX_FP32 solve hands every system
+ * over to its double-precision continuation after the first restart cycle
+ * (the path a system takes when single precision stops lowering its true
+ * residual). */
+#define DYFOX_BRAGG_FORCE_RESUME 1u
 
 /* Workspace bytes of dyfox_bragg_solve / dyfox_bragg_apply. */
 size_t dyfox_bragg_workspace_bytes(const dyfox_bragg_desc *d);

@@ -294,3 +294,19 @@ def test_wide_lateral_grids(gpu, diamond400, t, dx, half):
     r = max(float(np_(i64)[:, 0].max()), float(np_(i32)[:, 0].max()))
     assert r < 1e-4
     assert rel_l2(np_(o32), np_(o64)) < max(1e-8, 1e3 * r)
+
+
+def test_double_continuation_of_a_mixed_solve(gpu, diamond400, small):
+    """The path a system takes when single precision stalls: every system
+    of a mixed solve is handed over after its first restart cycle
+    (DYFOX_BRAGG_FORCE_RESUME) and finished in double from the solution
+    reached; the answers meet the tolerance and match the FP64 solve."""
+    from dyfox_gb300.bragg import FORCE_RESUME, solve_scan
+    b, cfg, seg, g = small
+    s = [float(b["s_dev"]), -1e5]
+    o64, _ = solve_scan(seg, s, cfg, b["ys"], diamond400, g)
+    o, info = solve_scan(seg, s, cfg, b["ys"], diamond400, g,
+                         precision="fp32", _flags=FORCE_RESUME)
+    info = np_(info)
+    assert info[:, 0].max() < 1e-10 and np.all(info[:, 2] == 0)
+    assert rel_l2(np_(o), np_(o64)) < 1e-8
