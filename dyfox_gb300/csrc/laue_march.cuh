@@ -144,6 +144,19 @@ __device__ __forceinline__ R two_sum(R a, R b, R &err) {
     return s;
 }
 
+// Dekker's Fast2Sum: s + err == a + b exactly when |a| >= |b| (round to
+// nearest).  In the march a is an amplitude and b its increment, at most
+// |kappa| ~ 0.02 of the other amplitude, so the sum is exact except near a
+// zero of the amplitude, where err is still b - (s - a) rounded: a
+// compensation no worse than none, at 3 operations instead of 6.
+template <typename R>
+__device__ __forceinline__ R fast_two_sum(R a, R b, R &err) {
+    R s = a + b;
+    err = b - (s - a);
+    return s;
+}
+constexpr bool kFastCompensation = true;
+
 __device__ __forceinline__ double fmaR(double a, double b, double c) {
     return fma(a, b, c);
 }
@@ -512,10 +525,18 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                 const R ur = fmaR(m21r, ar, fmaR(-m21i, ai, blr));
                 const R ui = fmaR(m21r, ai, fmaR(m21i, ar, bli));
                 R e0, e1, e2, e3;
-                Ar[j] = two_sum(ar, tr, e0); Alr[j] = e0;
-                Ai[j] = two_sum(ai, ti, e1); Ali[j] = e1;
-                Br[j] = two_sum(br, ur, e2); Blr[j] = e2;
-                Bi[j] = two_sum(bi, ui, e3); Bli[j] = e3;
+                if constexpr (kFastCompensation) {
+                    Ar[j] = fast_two_sum(ar, tr, e0);
+                    Ai[j] = fast_two_sum(ai, ti, e1);
+                    Br[j] = fast_two_sum(br, ur, e2);
+                    Bi[j] = fast_two_sum(bi, ui, e3);
+                } else {
+                    Ar[j] = two_sum(ar, tr, e0);
+                    Ai[j] = two_sum(ai, ti, e1);
+                    Br[j] = two_sum(br, ur, e2);
+                    Bi[j] = two_sum(bi, ui, e3);
+                }
+                Alr[j] = e0; Ali[j] = e1; Blr[j] = e2; Bli[j] = e3;
             }
         }
         const int q = p ^ 1;
