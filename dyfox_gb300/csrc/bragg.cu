@@ -539,17 +539,6 @@ __global__ void bragg_apply_kernel(const BraggArgs a, int mode,
 }
 
 // ---------------------------------------------------------------------------
-static FftPlan make_fft_plan(int N) {
-    FftPlan p;
-    memset(&p, 0, sizeof p);
-    p.n = N;
-    int n = N;
-    while (n % 4 == 0 && p.nfac < 24) { p.fac[p.nfac++] = 4; n /= 4; }
-    while (n % 2 == 0 && p.nfac < 24) { p.fac[p.nfac++] = 2; n /= 2; }
-    for (int f = 3; n > 1 && p.nfac < 24; f += 2)
-        while (n % f == 0 && p.nfac < 24) { p.fac[p.nfac++] = f; n /= f; }
-    return p;
-}
 
 struct BraggPlan {
     int threads, cpl;

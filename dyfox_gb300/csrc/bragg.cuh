@@ -9,6 +9,8 @@
 //     preconditioner ifft(fft(w) / T22s) of bragg/solver.py:167-168, in
 //     double and in single precision.
 #pragma once
+#include <string.h>
+
 #include "common.cuh"
 
 namespace dyfox {
@@ -232,6 +234,19 @@ struct FftPlan {
     int nfac;
     int fac[24];
 };
+
+// Radices of an N-point transform: 4s, then 2s, then odd factors.
+inline FftPlan make_fft_plan(int N) {
+    FftPlan p;
+    memset(&p, 0, sizeof p);
+    p.n = N;
+    int n = N;
+    while (n % 4 == 0 && p.nfac < 24) { p.fac[p.nfac++] = 4; n /= 4; }
+    while (n % 2 == 0 && p.nfac < 24) { p.fac[p.nfac++] = 2; n /= 2; }
+    for (int f = 3; n > 1 && p.nfac < 24; f += 2)
+        while (n % f == 0 && p.nfac < 24) { p.fac[p.nfac++] = f; n /= f; }
+    return p;
+}
 
 template <typename C>
 __device__ __forceinline__ C twid(const C *tw, int m, bool inv) {

@@ -35,8 +35,8 @@ typedef enum dyfox_status {
 } dyfox_status;
 
 /* Precision of a march.  FP64: plain double everywhere (parity mode).
- * FP32: single-precision march in the interaction picture with two-sum
- * compensated amplitude updates; per-segment Volterra terms and sincos in
+ * FP32: single-precision march in the interaction picture with compensated
+ * amplitude updates (Dekker Fast2Sum); per-segment Volterra terms and sincos in
  * single precision with offsets set up in double; the segment sum kept in
  * float-float (two-sum) and reduced mod 2 pi exactly (Cody-Waite), or in
  * double with DYFOX_FLAG_H_FP64. */
@@ -282,6 +282,40 @@ int dyfox_batch_kernel_count(const dyfox_batch *batch);
 
 /* Frees the graph and the plan (not the workspace). */
 int dyfox_batch_destroy(dyfox_batch *batch);
+
+/* ---- Imaging and rocking-scan maps -----------------------------------------
+ * Pupil of an objective on the fftshifted frequency grid (replaces
+ * Optics.pupil, optics.py:64-118): frequency (i - N/2) / (N dx) per axis;
+ * the aperture disc of radius aperture_f (NA / lambda) about (aperture_fx,
+ * aperture_fy); for ell != 0 the spiral phase ell atan2(fy - sy, fx - sx)
+ * about (singularity_fx, singularity_fy), quantised to `levels` steps when
+ * levels > 0; dc_zero != 0 zeroes the origin bin (the caller applies the
+ * reference's "exact" / "half_bin" / "never" policy).  pupil: device
+ * (Ny, Nx) complex128 (FP64) or complex64 (FP32). */
+int dyfox_pupil(int Nx, int Ny, double dx, double aperture_f, int ell,
+                double aperture_fx, double aperture_fy, double singularity_fx,
+                double singularity_fy, int dc_zero, int levels, int precision,
+                void *pupil, void *stream);
+
+/* Workspace bytes of dyfox_image for n images of Ny x Nx (even sizes). */
+int dyfox_image_workspace_bytes(int n, int Ny, int Nx, int precision,
+                                size_t *bytes);
+
+/* Image-plane intensity of n exit waves through one pupil (replaces
+ * image_intensity / object_spectrum / image_from_spectrum, optics.py:
+ * 170-207): I = |ifft2(fft2(u) ifftshift(P))|^2, equal to the reference's
+ * shifted composition for even Ny, Nx.  stack: device (n, Ny, Nx) complex
+ * of `precision` (unchanged); pupil: as dyfox_pupil, same precision.
+ * out (may be NULL): device (n, Ny, Nx) float64 / float32.  With sum_I !=
+ * NULL the images are also reduced as com_maps does (analysis/rocking.py:
+ * 37-83): sum_I[y][x] += I, sum_wI[y][x] += phi[e] I (device (Ny, Nx)
+ * doubles, accumulated across calls, images in order: deterministic), and
+ * rock (device n doubles, may be NULL) receives sum_xy I per image; phi:
+ * device n doubles. */
+int dyfox_image(const void *stack, int n, int Ny, int Nx, int precision,
+                const void *pupil, void *out, const double *phi,
+                double *sum_wI, double *sum_I, double *rock, void *workspace,
+                size_t workspace_bytes, void *stream);
 
 /* ---- Learned shooting guess (no DYFOX counterpart) ------------------------
  * A 4-level U-Net, 32 base channels, bfloat16 storage and FP32 accumulation

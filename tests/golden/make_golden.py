@@ -22,13 +22,62 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 
 
+def optics_golden():
+    """Pupils and images from the reference's optics.py (NumPy): an
+    Optics of the Diamond (400) 17 keV crystal on a 32 x 48 grid, charges
+    0, 2 and -1, offsets of the singularity and of the aperture, phase
+    levels, the three DC policies; images of a seeded stack of 3 exit waves
+    through three of the pupils."""
+    from crystal import DIAMOND, CrystalParams
+    from optics import Optics, image_intensity
+    x = CrystalParams.from_reflection(DIAMOND, (4, 0, 0), 17.0,
+                                      f_prime=0.003, f_dprime=0.002,
+                                      label="Diamond(400)")
+    Ny, Nx, dx = 32, 48, 0.25e-6
+    lens = Optics(NA=6e-5, f_lens=0.274, xtal=x, xp=np)
+    step = 1.0 / (Nx * dx)
+    cases = [  # (ell, aperture_f, singularity_f, dc_zero, levels)
+        (0, (0.0, 0.0), (0.0, 0.0), "exact", 0),
+        (2, (0.0, 0.0), (0.0, 0.0), "exact", 0),
+        (-1, (0.0, 0.0), (0.0, 0.0), "never", 0),
+        (2, (0.0, 0.0), (0.3 * step, -0.2 * step), "half_bin", 0),
+        (1, (0.0, 0.0), (0.7 * step, 0.0), "half_bin", 0),
+        (2, (1.5 * step, 0.0), (1.5 * step, 0.0), "never", 0),
+        (3, (0.0, 2.0 * step), (0.0, 0.0), "exact", 4),
+    ]
+    pupils = np.array([lens.pupil(Nx, Ny, dx, ell, aperture_f=af,
+                                  singularity_f=sf, dc_zero=dc, levels=lv,
+                                  cache=False)
+                       for ell, af, sf, dc, lv in cases])
+    rng = np.random.default_rng(20260909)
+    stack = (rng.normal(size=(3, Ny, Nx))
+             + 1j * rng.normal(size=(3, Ny, Nx)))
+    images = np.array([image_intensity(stack, pupils[k]) for k in (0, 1, 3)])
+    phi = np.array([-12.5, 0.0, 40.0])
+    np.savez_compressed(os.path.join(HERE, "optics_small.npz"),
+                        Ny=Ny, Nx=Nx, dx=dx, NA=6e-5, f_lens=0.274,
+                        lam=x.lam, case_ell=np.array([c[0] for c in cases]),
+                        case_aperture=np.array([c[1] for c in cases]),
+                        case_singularity=np.array([c[2] for c in cases]),
+                        case_dc=np.array([c[3] for c in cases]),
+                        case_levels=np.array([c[4] for c in cases]),
+                        pupils=pupils, stack=stack, images=images,
+                        image_pupils=np.array([0, 1, 3]), phi=phi)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", choices=["optics"], default=None,
+                    help="write only this fixture")
     args = ap.parse_args()
     sys.dont_write_bytecode = True
     sys.path.insert(0, ROOT)
     sys.path.insert(0, args.reference)
+    if args.only == "optics":
+        optics_golden()
+        print("optics fixture written to", HERE)
+        return
     import subprocess
     subprocess.check_call([sys.executable, os.path.join(ROOT, "oracle",
                                                         "make_ref.py"),
@@ -202,6 +251,7 @@ def main():
              riccati_urad=urad_r,
              riccati_6um=reflectivity_riccati(sd_r, bc.t_crystal, x),
              semi_inf=reflectivity_semi_infinite(sd_r, x))
+    optics_golden()
     print("golden fixtures written to", HERE)
 
 
