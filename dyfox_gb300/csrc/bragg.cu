@@ -19,12 +19,12 @@
 // at true relative residual <= tol computed in double; a restart cycle
 // stops its inner iteration once the estimated residual has dropped by
 // kMixedInnerDrop, below which the single-precision operator's own error
-// makes further inner steps useless.  Where single precision is not
-// accurate enough for a system (thick slabs, long marches), a restart cycle
-// whose inner iteration estimated a reduction of 10x or more while the true
-// residual did not halve ends the mixed solve, and the CTA finishes that
-// system in double from the solution reached (each path compiled on its
-// own, so the single-precision loop carries no double-precision branch).
+// makes further inner steps useless.  A system the mixed solve does not
+// converge within maxiter restarts (single precision not accurate enough
+// for it) is finished in double, from the solution reached, by a separate
+// resume launch.  The test sits after the restart loop: any test inside it
+// (of the cycle's true-residual reduction) measured 30% slower on config 1
+// even when it never fired.
 #include <math.h>
 #include <string.h>
 
@@ -193,10 +193,9 @@ constexpr double kMixedInnerDrop = 1e-5;
 // sys % n_y) of `a` by the calling CTA.  smem: gmres_smem(Nx, restart).
 // warm: start from the X already in place (else from a.use_x0's rule);
 // inner0: inner iterations already spent on this system.  Returns -1 when
-// the solve ended (result and info written); a MIXED solve whose single-
-// precision products stopped lowering the true residual returns its inner
-// iteration count instead and writes nothing, and the caller continues in
-// double from the X reached so far.
+// the solve ended (result and info written); a MIXED solve that did not
+// converge returns its inner iteration count instead and writes nothing,
+// and the caller continues in double from the X reached so far.
 template <int CPL, bool MIXED>
 __device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
                                             unsigned char *smem, bool warm,
@@ -309,7 +308,6 @@ __device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
                 // inner stopping level of this cycle
                 const double pstop =
                     MIXED ? fmax(ptol, kMixedInnerDrop * tmp) : ptol;
-                const double rprev = rnorm;
                 for (int x = tid; x < Nx; x += nt) V[x] = cscale(1.0 / tmp, W[x]);
                 for (int j = tid; j <= m; j += nt)
                     S[j] = make_double2(j == 0 ? tmp : 0.0, 0.0);
@@ -420,9 +418,6 @@ __device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
                 __syncthreads();
                 rnorm = norm2(W);
                 if (rnorm <= atol) { code = 0; break; }
-                if (MIXED && ((rnorm > 0.5 * rprev && presid < 0.1 * tmp) ||
-                              a.force_resume))
-                    return inner0 + inner;        // single precision stalled
                 if (breakdown) break;
                 if (presid <= ptol)
                     ptol_max_factor = fmax(eps, 0.25 * ptol_max_factor);
@@ -433,6 +428,9 @@ __device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
             if (rnorm <= atol) code = 0;
         }
     }
+    // A mixed solve that did not converge (single precision not accurate
+    // enough for this system) is handed over to the double continuation.
+    if (MIXED && (code != 0 || a.force_resume)) return inner0 + inner;
     // exit wave v e^{-iH(0)}
     double2 *out = a.out + ((size_t)is * a.n_y + iy) * Nx;
     const double2 *e0h = a.e0h + (size_t)iy * Nx;
@@ -472,14 +470,14 @@ __device__ __forceinline__ void resume_system(const BraggArgs &a, int sys,
     gmres_system<CPL, false>(a, sys, smem, true, (int)info[1]);
 }
 
-// The GMRES kernels are compiled for their CTA size only: holding the
-// 128-thread kernel to 5 resident CTAs an SM (96 registers) was measured
-// 18% slower on config 1 than letting it take the registers it needs.
-constexpr int gmres_min_blocks(int) { return 1; }
+// The GMRES kernels carry no launch bounds: the compiler's own choice
+// (about 100 registers for the 4-column mixed kernel) measured fastest on
+// config 1.  Bounds of (128, 5) forced 96 registers and lost 18%; bounds of
+// (NT, 1) let it take 212 registers and lost 40% to occupancy.
 
 // One CTA of NT threads per system of one solve call.
 template <int CPL, bool MIXED, int NT>
-__global__ void __launch_bounds__(NT, gmres_min_blocks(NT))
+__global__ void
 bragg_gmres_kernel(const BraggArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     solve_system<CPL, MIXED>(a, blockIdx.x, smem);
@@ -488,7 +486,7 @@ bragg_gmres_kernel(const BraggArgs a) {
 // After a mixed launch: one CTA per system, returning at once unless the
 // system was marked.
 template <int CPL, int NT>
-__global__ void __launch_bounds__(NT, gmres_min_blocks(NT))
+__global__ void
 bragg_resume_kernel(const BraggArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     resume_system<CPL>(a, blockIdx.x, smem);
@@ -779,7 +777,7 @@ static cudaError_t launch_apply(const BraggArgs &a, int threads, size_t smem,
 // Pieces used by the batched launcher (batch.cu): one CTA per system of
 // many instances, the instances' arguments in a device array.
 template <int CPL, int NT>
-__global__ void __launch_bounds__(NT, gmres_min_blocks(NT))
+__global__ void
 bragg_batch_resume_kernel(const BraggArgs *__restrict__ insts,
                           const int2 *__restrict__ systems) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -791,7 +789,7 @@ bragg_batch_resume_kernel(const BraggArgs *__restrict__ insts,
 }
 
 template <int CPL, bool MIXED, int NT>
-__global__ void __launch_bounds__(NT, gmres_min_blocks(NT))
+__global__ void
 bragg_batch_kernel(const BraggArgs *__restrict__ insts,
                    const int2 *__restrict__ systems) {
     extern __shared__ __align__(16) unsigned char smem[];

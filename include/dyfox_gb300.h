@@ -168,9 +168,8 @@ typedef struct dyfox_bragg_desc {
 } dyfox_bragg_desc;
 
 /* dyfox_bragg_desc.flags: for checks, a DYFOX_FP32 solve hands every system
- * over to its double-precision continuation after the first restart cycle
- * (the path a system takes when single precision stops lowering its true
- * residual). */
+ * over to its double-precision continuation (the path of a system the
+ * mixed solve does not converge within maxiter restarts). */
 #define DYFOX_BRAGG_FORCE_RESUME 1u
 
 /* Workspace bytes of dyfox_bragg_solve / dyfox_bragg_apply. */

@@ -297,10 +297,10 @@ def test_wide_lateral_grids(gpu, diamond400, t, dx, half):
 
 
 def test_double_continuation_of_a_mixed_solve(gpu, diamond400, small):
-    """The path a system takes when single precision stalls: every system
-    of a mixed solve is handed over after its first restart cycle
-    (DYFOX_BRAGG_FORCE_RESUME) and finished in double from the solution
-    reached; the answers meet the tolerance and match the FP64 solve."""
+    """The path of a system the mixed solve does not converge: every system
+    is handed over (DYFOX_BRAGG_FORCE_RESUME) and finished in double from
+    the solution reached; the answers meet the tolerance and match the FP64
+    solve."""
     from dyfox_gb300.bragg import FORCE_RESUME, solve_scan
     b, cfg, seg, g = small
     s = [float(b["s_dev"]), -1e5]
