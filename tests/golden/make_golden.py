@@ -65,10 +65,52 @@ def optics_golden():
                         image_pupils=np.array([0, 1, 3]), phi=phi)
 
 
+def host_rows_golden():
+    """Cache keys of the reference's laue/cache.py WaveCache and the
+    nodes of its illumination.py, for a few inputs."""
+    import json
+    from backend import FP32, FP64
+    from crystal import DIAMOND, CrystalParams
+    from dislocations import burgers_vector, straight_segment
+    from illumination import (condenser_angles, convergence_bandwidth_nodes,
+                              gauss_hermite_offsets)
+    from laue import LaueGrid
+    from laue.cache import WaveCache
+    x = CrystalParams.from_reflection(DIAMOND, (4, 0, 0), 17.0,
+                                      f_prime=0.003, f_dprime=0.002,
+                                      label="Diamond(400)")
+    grid = LaueGrid(x, t_crystal=200e-6, dx=0.25e-6, beam_width=120e-6)
+    b = burgers_vector(x.U_lab, [1, 0, -1], x.b_mag, +1)
+    seg = straight_segment(np.array([1.0, 0.0, 1.0]) / np.sqrt(2.0), b,
+                           [0.0, 0.0, 100e-6], 800e-6)
+    keys = []
+    for cache, prec, s in ((WaveCache("w"), FP64, [0.0, 1e3]),
+                           (WaveCache("w"), FP32, [0.0, 1e3]),
+                           (WaveCache("w", store_dtype=np.complex128), FP64,
+                            [-2.5e3]),
+                           (WaveCache("w", version=8), FP64, [0.0])):
+        keys.append(cache.key(seg, s, grid, x, prec))
+    a, wa = condenser_angles(3.6)
+    offs, wo = gauss_hermite_offsets(1.5e-6, n=5)
+    out = {}
+    for name, kw in (("plain", {}), ("psi", {"matched": "psi"}),
+                     ("delta", {"matched": "delta"}),
+                     ("vignette", {"vignette_f": 2.0e4})):
+        S, D, W, info = convergence_bandwidth_nodes(
+            x, 20e-6, 1e-4, 9, 40e-6, 7, 3e-4, **kw)
+        out[name + "_S"], out[name + "_D"], out[name + "_W"] = S, D, W
+        out[name + "_info"] = json.dumps(info, sort_keys=True)
+    np.savez_compressed(os.path.join(HERE, "host_rows.npz"),
+                        cache_keys=np.array(keys), seg=np.array(
+                            [np.concatenate([np.asarray(q, float)
+                                             for q in seg[0]])]),
+                        cond_a=a, cond_w=wa, gh_offs=offs, gh_w=wo, **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["optics"], default=None,
+    ap.add_argument("--only", choices=["optics", "host_rows"], default=None,
                     help="write only this fixture")
     args = ap.parse_args()
     sys.dont_write_bytecode = True
@@ -77,6 +119,10 @@ def main():
     if args.only == "optics":
         optics_golden()
         print("optics fixture written to", HERE)
+        return
+    if args.only == "host_rows":
+        host_rows_golden()
+        print("host_rows fixture written to", HERE)
         return
     import subprocess
     subprocess.check_call([sys.executable, os.path.join(ROOT, "oracle",
@@ -252,6 +298,7 @@ def main():
              riccati_6um=reflectivity_riccati(sd_r, bc.t_crystal, x),
              semi_inf=reflectivity_semi_infinite(sd_r, x))
     optics_golden()
+    host_rows_golden()
     print("golden fixtures written to", HERE)
 
 
