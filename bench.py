@@ -212,7 +212,8 @@ def run_ours(args):
     if not args.no_tune and not args.once:
         for name, prec in (("fp32", FP32), ("fp64", FP64)):
             r = tune(seg, s, grid, x, precision=prec, h_mode="fused")
-            tuned[name] = {"cols_per_lane": r["cols_per_lane"],
+            tuned[name] = {"pairs": r.get("pairs", False),
+                           "cols_per_lane": r["cols_per_lane"],
                            "angles_per_cta": r["angles_per_cta"]}
 
     def make(prec, extra=0):
@@ -220,7 +221,9 @@ def run_ours(args):
                   flags=_lib.FLAG_FUSED | extra)
         shape = lookup(d)
         if shape is not None:
-            d.cols_per_lane, d.angles_per_cta = shape
+            d.cols_per_lane, d.angles_per_cta, pairs = shape
+            if pairs:
+                d.flags |= _lib.FLAG_PAIRS
         nb = L.dyfox_laue_workspace_bytes(d)
         ws = torch.empty(max(nb, 256), dtype=torch.uint8, device="cuda")
         out = torch.empty((n_e, geo["Ny"], geo["Nx"]),

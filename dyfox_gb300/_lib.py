@@ -18,6 +18,7 @@ DYFOX_FP64, DYFOX_FP32 = 0, 1
 H_NONE, H_GRID_F64, H_GRID_F32, H_SEGMENTS, H_ANALYTIC = 0, 1, 2, 3, 4
 FLAG_FUSED, FLAG_STAGED, FLAG_NO_COMP, FLAG_GENERAL = 1, 2, 4, 8
 FLAG_H_FP64 = 16
+FLAG_PAIRS, FLAG_SCALAR = 32, 64
 SEG_STRIDE = 24
 
 

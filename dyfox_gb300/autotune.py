@@ -1,10 +1,15 @@
 """Launch-shape autotuner of the Laue march.
 
 The register-resident march has two free shape parameters: columns per lane
-(CPL, the register tile of one thread: 4-8 in FP64, 5-13 in FP32) and
-angles per CTA (how many deviation parameters share one e^{iH} row, each
-with WA = ceil(Nx / (32 CPL)) warps).  The best pair depends on Nx, on the
-number of angles, on the H source and on the precision.  ``tune`` times the
+(CPL, the register tile of one thread: 4-8 in FP64, 5-13 in FP32, 3-7 in
+the packed-pair FP32 march) and angles per CTA (how many deviation
+parameters share one e^{iH} row, each with WA = ceil(Nx / (32 CPL)) warps,
+or each pair of them in the pair march).  The best shape depends on Nx, on
+the number of angles, on the H source and on the precision.  The pair march
+is timed only when asked (``pairs=True``): on GB300 it has run about 10%
+behind the scalar march on the README and rocking-scan workloads, since a
+packed FFMA2 issues once but occupies the FP32 pipe for two operations.
+``tune`` times the
 candidates on a copy of the grid cut down in rows (same Nx and Nz, so the
 per-row work is unchanged) but with about 2048 CTAs per candidate, enough to
 fill the GPU as the full problem does, compares time per row, keeps the
@@ -25,6 +30,8 @@ from . import _lib
 
 CPL = {"fp64": (4, 5, 6, 7, 8), "fp32": (5, 7, 9, 11, 13)}
 ANGLES = (1, 2, 3, 4, 6, 8)
+CPL_PAIRS = (3, 5, 7)
+ANGLES_PAIRS = (2, 4, 6, 8)
 _lock = threading.Lock()
 _cache = None
 
@@ -65,24 +72,29 @@ def _bucket(n):
 def signature(desc):
     torch = _lib.torch_cuda()
     name = torch.cuda.get_device_name()
+    flags = desc.flags & ~(_lib.FLAG_GENERAL | _lib.FLAG_PAIRS |
+                           _lib.FLAG_SCALAR)
     return "|".join(str(v) for v in (
-        name, desc.precision, desc.h_source, desc.flags & ~_lib.FLAG_GENERAL,
+        name, desc.precision, desc.h_source, flags,
         desc.Nx, desc.Nz, _bucket(desc.n_e), _bucket(desc.n_seg)))
 
 
 def lookup(desc):
-    """(cols_per_lane, angles_per_cta) cached for this signature, or None."""
+    """(cols_per_lane, angles_per_cta, pairs) cached for this signature,
+    or None."""
     with _lock:
         e = _load().get(signature(desc))
-    return None if e is None else (e["cols_per_lane"], e["angles_per_cta"])
+    return None if e is None else (e["cols_per_lane"], e["angles_per_cta"],
+                                   bool(e.get("pairs", False)))
 
 
 def tune(seg_list, s_dev_arr, grid, xtal, *, precision="fp32",
          h_mode="auto", H_gpu=None, compensated=True, h_sum="ff", ctas=2048,
-         repeats=3, verbose=False):
-    """Time every (CPL, angles per CTA) candidate for this problem and cache
-    the fastest.  Returns {"cols_per_lane", "angles_per_cta", "ms",
-    "candidates": [(cpl, A, ms), ...]}."""
+         repeats=3, verbose=False, pairs=False):
+    """Time every (CPL, angles per CTA, pair march) candidate for this
+    problem and cache the fastest.  Returns {"cols_per_lane",
+    "angles_per_cta", "pairs", "ms", "candidates": [(cpl, A, pairs, ms),
+    ...]}."""
     from .backend import precision as as_precision
     from .grid import grid_arrays
     from .laue import _solve
@@ -95,51 +107,54 @@ def tune(seg_list, s_dev_arr, grid, xtal, *, precision="fp32",
     results = []
     ev0, ev1 = torch.cuda.Event(enable_timing=True), \
         torch.cuda.Event(enable_timing=True)
-    for cpl in CPL[prec.name]:
+    shapes = [(cpl, A, False) for cpl in CPL[prec.name] for A in ANGLES]
+    if pairs and prec.is_fp32 and compensated and len(s) >= 2:
+        shapes += [(cpl, A, True) for cpl in CPL_PAIRS for A in ANGLES_PAIRS]
+    for cpl, A, pairs in shapes:
         if -(-full["Nx"] // (32 * cpl)) > 32:
             continue
-        for A in ANGLES:
-            if A > len(s):
-                continue
-            groups = -(-len(s) // A)
-            rows = min(full_rows, max(32, -(-ctas // groups)))
-            small = grid if (H_gpu is not None or rows >= full_rows) else \
-                grid.replace(beam_width=rows * grid.dx)
-            geo = grid_arrays(small)
-            n_rows = int(np.sum(np.abs((np.arange(geo["Ny"]) - geo["Ny"] // 2)
-                                       * geo["dx"]) < geo["fov_hy"]))
-            out = torch.empty((len(s), geo["Ny"], geo["Nx"]),
-                              dtype=prec.torch_complex, device="cuda")
-            try:
-                kw = dict(h_mode=h_mode, angles_per_cta=A, cols_per_lane=cpl,
-                          out=out, tuned=False, compensated=compensated,
-                          h_sum=h_sum)
-                _solve(seg_list, s, small, xtal, H_gpu, 0, prec, False, **kw)
+        if A > len(s) + (1 if pairs else 0):
+            continue
+        groups = -(-len(s) // A)
+        rows = min(full_rows, max(32, -(-ctas // groups)))
+        small = grid if (H_gpu is not None or rows >= full_rows) else \
+            grid.replace(beam_width=rows * grid.dx)
+        geo = grid_arrays(small)
+        n_rows = int(np.sum(np.abs((np.arange(geo["Ny"]) - geo["Ny"] // 2)
+                                   * geo["dx"]) < geo["fov_hy"]))
+        out = torch.empty((len(s), geo["Ny"], geo["Nx"]),
+                          dtype=prec.torch_complex, device="cuda")
+        try:
+            kw = dict(h_mode=h_mode, angles_per_cta=A, cols_per_lane=cpl,
+                      out=out, tuned=False, compensated=compensated,
+                      h_sum=h_sum, pairs=pairs)
+            _solve(seg_list, s, small, xtal, H_gpu, 0, prec, False, **kw)
+            torch.cuda.synchronize()
+            best = np.inf
+            for _ in range(repeats):
+                ev0.record()
+                _solve(seg_list, s, small, xtal, H_gpu, 0, prec, False,
+                       **kw)
+                ev1.record()
                 torch.cuda.synchronize()
-                best = np.inf
-                for _ in range(repeats):
-                    ev0.record()
-                    _solve(seg_list, s, small, xtal, H_gpu, 0, prec, False,
-                           **kw)
-                    ev1.record()
-                    torch.cuda.synchronize()
-                    best = min(best, ev0.elapsed_time(ev1))
-            except (ValueError, NotImplementedError, MemoryError):
-                continue
-            results.append((cpl, A, best / n_rows * full_rows))
-            if verbose:
-                print(f"cpl {cpl:2d} angles/CTA {A}: {best:.3f} ms on "
-                      f"{n_rows} rows, {results[-1][2]:.3f} ms scaled")
+                best = min(best, ev0.elapsed_time(ev1))
+        except (ValueError, NotImplementedError, MemoryError):
+            continue
+        results.append((cpl, A, pairs, best / n_rows * full_rows))
+        if verbose:
+            print(f"cpl {cpl:2d} angles/CTA {A} pairs {pairs}: "
+                  f"{best:.3f} ms on {n_rows} rows, "
+                  f"{results[-1][3]:.3f} ms scaled")
     if not results:
         raise RuntimeError("no launch shape could run this problem")
-    cpl, A, ms = min(results, key=lambda r: r[2])
+    cpl, A, pairs, ms = min(results, key=lambda r: r[3])
     from .laue import describe
     d = describe(seg_list, s, grid, xtal, H_gpu=H_gpu, precision=prec,
                  h_mode=h_mode, compensated=compensated, h_sum=h_sum)
     with _lock:
         _load()[signature(d)] = {"cols_per_lane": cpl, "angles_per_cta": A,
-                                 "ms_full_estimate": ms}
+                                 "pairs": pairs, "ms_full_estimate": ms}
         _save()
-    return {"cols_per_lane": cpl, "angles_per_cta": A, "ms": ms,
-            "candidates": results}
+    return {"cols_per_lane": cpl, "angles_per_cta": A, "pairs": pairs,
+            "ms": ms, "candidates": results}
 

@@ -34,7 +34,7 @@ int laue_check_desc(const dyfox_laue_desc *d);
 void laue_active_rows(const dyfox_laue_desc *d, int *row0, int *n_rows);
 cudaError_t launch_laue_setup(const dyfox_laue_desc *d, const double *s_dev,
                               Kappa *kappa, float4 *kappa32, double2 *scale,
-                              cudaStream_t stream);
+                              float4 *kpair, cudaStream_t stream);
 cudaError_t launch_zero_rows(const dyfox_laue_desc *d, void *out, size_t elem,
                              int row0, int n_rows, cudaStream_t stream);
 // bragg.cu
@@ -372,7 +372,8 @@ static int record_batch(const dyfox_batch_item *items, const BatchLayout &L,
         if ((e = launch_laue_setup(d, items[b.item].s_dev,
                                    (Kappa *)(ws + b.off_kappa),
                                    (float4 *)(ws + b.off_k32),
-                                   (double2 *)(ws + b.off_scale), s)))
+                                   (double2 *)(ws + b.off_scale), nullptr,
+                                   s)))
             return cuda_status(e, "laue_setup");
     }
     for (size_t j = 0; j < L.bragg.size(); ++j) {

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include "laue_march.cuh"
+#include "laue_pair.cuh"
 
 namespace dyfox {
 
@@ -27,7 +28,8 @@ __global__ void laue_setup_kernel(const double *__restrict__ s_dev, int n_e,
                                   int nsteps, double ds, double s0r,
                                   double s0i, double shr, double shi,
                                   double sbr, double sbi, Kappa *kappa,
-                                  float4 *kappa32, double2 *scale) {
+                                  float4 *kappa32, double2 *scale,
+                                  float *kpair) {
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (idx >= (long)n_e * nsteps) return;
     const int ie = (int)(idx / nsteps), k = (int)(idx - (long)ie * nsteps);
@@ -59,6 +61,20 @@ __global__ void laue_setup_kernel(const double *__restrict__ s_dev, int n_e,
     kappa[idx] = kp;
     kappa32[idx] = make_float4((float)kp.k12.x, (float)kp.k12.y,
                                (float)kp.k21.x, (float)kp.k21.y);
+    if (kpair) {
+        // This angle's half of its pair's KPair (laue_pair.cuh); the last
+        // angle of an odd count fills both halves.
+        const float k12r = (float)kp.k12.x, k12i = (float)kp.k12.y;
+        const float k21r = (float)kp.k21.x, k21i = (float)kp.k21.y;
+        float *q = kpair + ((size_t)(ie >> 1) * nsteps + k) * 16;
+        const int t0 = ie & 1, t1 = (ie == n_e - 1 && t0 == 0) ? 1 : t0;
+        for (int t = t0; t <= t1; ++t) {
+            q[0 + t] = k12r;   q[2 + t] = k12i;
+            q[4 + t] = -k12i;  q[6 + t] = -k12r;
+            q[8 + t] = k21r;   q[10 + t] = k21i;
+            q[12 + t] = -k21r; q[14 + t] = -k21i;
+        }
+    }
     if (k == 0) {
         const double exp_pr = exp(s0r * ds);
         const double pi_ = (s0i + alpha * 0.5) * ds;
@@ -205,7 +221,7 @@ struct LauePlan {
     int stage = 0;           // 0: none, 1: stage e^{iH} (CS32/CS64)
     int row0 = 0, n_rows = 0;
     size_t off_kappa = 0, off_k32 = 0, off_scale = 0, off_stage = 0,
-           off_piv = 0, ws = 0;
+           off_piv = 0, off_kpair = 0, ws = 0;
 };
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -313,6 +329,10 @@ static int make_plan(const dyfox_laue_desc *d, LauePlan *p) {
     if (p->hsrc == HS_SEG && single)
         off = align256(off + (size_t)p->n_rows * (d->Nz - 1) * d->n_seg *
                                  sizeof(float4));
+    p->off_kpair = off;
+    if (single)
+        off = align256(off + (size_t)((d->n_e + 1) / 2) * (d->Nz - 1) *
+                                 sizeof(KPair));
     p->ws = off;
     return DYFOX_OK;
 }
@@ -322,7 +342,29 @@ struct FastConfig {
     int cpl, WA, A, block;
     size_t smem;
     int stage = ST_COMPUTE, raw_elem = 0;
+    bool pairs = false;      // A counts angle pairs
 };
+
+// The packed-pair march (laue_pair.cuh) applies to compensated single
+// precision with the fused segment phase or staged float2 e^{iH} rows, at
+// two or more deviation parameters; DYFOX_FLAG_PAIRS selects it there (a
+// cols_per_lane it does not have keeps the scalar march).
+static bool use_pairs(const dyfox_laue_desc *d, const LauePlan &p,
+                      const FastConfig &fc) {
+    if (d->precision != DYFOX_FP32 || (d->flags & DYFOX_FLAG_NO_COMP) ||
+        !(d->flags & DYFOX_FLAG_PAIRS) || (d->flags & DYFOX_FLAG_SCALAR) ||
+        d->n_e < 2)
+        return false;
+    if (!(p.hsrc == HS_SEG || (p.hsrc == HS_CS32 && fc.stage == ST_DIRECT)))
+        return false;
+    if (d->cols_per_lane) {
+        bool have = false;
+        for (int i = 0; i < kNumCplPair; ++i)
+            have = have || kCplPair[i] == d->cols_per_lane;
+        if (!have) return false;
+    }
+    return true;
+}
 
 static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
                        FastConfig *fc) {
@@ -331,8 +373,9 @@ static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
     const int ht = p.hsrc != HS_SEG ? HT_GENERIC
                    : (single && (d->flags & DYFOX_FLAG_H_FP64)) ? HT_SEG64
                                                                 : HT_SEG;
-    const int *cpls = single ? kCplF32 : kCplF64;
-    const int ncpl = single ? kNumCplF32 : kNumCplF64;
+    fc->pairs = use_pairs(d, p, *fc);
+    const int *cpls = fc->pairs ? kCplPair : single ? kCplF32 : kCplF64;
+    const int ncpl = fc->pairs ? kNumCplPair : single ? kNumCplF32 : kNumCplF64;
     // Columns per lane: the fewest padded columns; ties go to more columns
     // per lane (fewer warps per angle).
     int best = -1, best_pad = 1 << 30;
@@ -354,9 +397,10 @@ static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
     }
     fc->cpl = best;
     fc->WA = div_up(d->Nx, 32 * best);
-    fc->entry = single ? (comp ? march_entry_f32_comp(best, ht)
-                               : march_entry_f32_plain(best, ht))
-                       : march_entry_f64(best, ht);
+    fc->entry = fc->pairs ? march_entry_f32_pair(best, ht)
+                : single ? (comp ? march_entry_f32_comp(best, ht)
+                                 : march_entry_f32_plain(best, ht))
+                         : march_entry_f64(best, ht);
     if (!fc->entry.launch) {
         set_error("missing instantiation cpl=%d", best);
         return DYFOX_ENOSYS;
@@ -374,15 +418,23 @@ static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
                   d->Nx, fc->WA);
         return DYFOX_ENOSYS;
     }
-    int A = d->angles_per_cta > 0 ? d->angles_per_cta : d->n_e;
+    // Angles (pairs of angles for the pair march) per CTA.
+    const int units = fc->pairs ? (d->n_e + 1) / 2 : d->n_e;
+    int A = d->angles_per_cta > 0
+                ? (fc->pairs ? (d->angles_per_cta + 1) / 2 : d->angles_per_cta)
+                : units;
     if (A > amax) A = amax;
-    if (A > d->n_e) A = d->n_e;
+    if (A > units) A = units;
     if (A * 32 * fc->WA > max_threads) {
         set_error("angles_per_cta=%d exceeds the block limit", A);
         return DYFOX_EINVAL;
     }
     fc->A = A;
     fc->block = 32 * fc->WA * A;
+    if (fc->pairs) {
+        fc->smem = pair_smem(best, fc->WA, A, d->n_seg, p.hsrc == HS_SEG).total;
+        return DYFOX_OK;
+    }
     MarchSmem sm = single
         ? march_smem<float>(best, fc->WA, A, d->Nz, p.hsrc, d->n_seg, comp,
                             fc->stage, fc->raw_elem)
@@ -438,12 +490,13 @@ void laue_active_rows(const dyfox_laue_desc *d, int *row0, int *n_rows) {
 
 cudaError_t launch_laue_setup(const dyfox_laue_desc *d, const double *s_dev,
                               Kappa *kappa, float4 *kappa32, double2 *scale,
-                              cudaStream_t stream) {
+                              float4 *kpair, cudaStream_t stream) {
     const int nsteps = d->Nz - 1;
     const long n = (long)d->n_e * nsteps;
     laue_setup_kernel<<<(int)((n + 255) / 256), 256, 0, stream>>>(
         s_dev, d->n_e, nsteps, d->ds, d->sig0[0], d->sig0[1], d->sig_h[0],
-        d->sig_h[1], d->sig_hbar[0], d->sig_hbar[1], kappa, kappa32, scale);
+        d->sig_h[1], d->sig_hbar[0], d->sig_hbar[1], kappa, kappa32, scale,
+        reinterpret_cast<float *>(kpair));
     count_launch(1);
     return cudaGetLastError();
 }
@@ -518,6 +571,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     a.out = out;
     a.csgrid = ws + p.off_stage;
     a.piv = (const float4 *)(ws + p.off_piv);
+    a.kpair = single ? (const float4 *)(ws + p.off_kpair) : nullptr;
 
     cudaError_t e;
     // Rows outside the beam are zero.
@@ -526,7 +580,9 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     if (p.n_rows == 0) return DYFOX_OK;
     if ((e = launch_laue_setup(d, s_dev, (Kappa *)(ws + p.off_kappa),
                                (float4 *)(ws + p.off_k32),
-                               (double2 *)(ws + p.off_scale), stream)))
+                               (double2 *)(ws + p.off_scale),
+                               single ? (float4 *)(ws + p.off_kpair) : nullptr,
+                               stream)))
         return cuda_status(e, "laue_setup");
     if (p.hsrc == HS_SEG && single) {
         const long n = (long)p.n_rows * nsteps * d->n_seg;
@@ -582,7 +638,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     a.WA = fc.WA;
     a.A = fc.A;
     a.ncols = 32 * fc.WA * fc.cpl;
-    a.n_groups = div_up(d->n_e, fc.A);
+    a.n_groups = div_up(fc.pairs ? (d->n_e + 1) / 2 : d->n_e, fc.A);
     a.stage = fc.stage;
     a.raw_elem = fc.raw_elem;
     e = fc.entry.launch(a, p.n_rows * a.n_groups, fc.block, fc.smem, stream);

@@ -67,6 +67,7 @@ struct MarchArgs {
     double an[12];              // ANALYTIC
     const Kappa *kappa;         // (n_e, Nz - 1): kappa12, kappa21
     const float4 *kappa32;      // the same, rounded to float (FP32 march)
+    const float4 *kpair;        // pair march: (n_e + 1) / 2 x (Nz - 1) KPair
     const double2 *scale;       // (n_e): M22^(Nz-1)
     void *out;                  // (n_e, Ny, Nx) complex (R2)
     int stage;                  // StageMode of a GENERIC source
@@ -228,6 +229,48 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// e^{iH} (cos, sin) of column x in single precision from the segment
+// constants and the row's pivots.  HT_SEG: float-float sum started at the
+// reduced constant hcr, reduced mod 2 pi in float-float; HT_SEG64: double
+// sum started at the constant hconst, reduced in double.
+template <int HT>
+__device__ __forceinline__ float2 seg_phase_one(const SegF &f, float4 p0,
+                                                int x, float hcr,
+                                                double hconst) {
+    const float h = h_seg_f32(f, p0, x);
+    if constexpr (HT == HT_SEG) {
+        float e;
+        const float hi = two_sum(hcr, h, e);
+        float sn, c;
+        __sincosf(reduce_2pi_ff(hi, e), &sn, &c);
+        return make_float2(c, sn);
+    } else {
+        return CS<float>::of_f64(hconst + (double)h);
+    }
+}
+
+template <int HT>
+__device__ __forceinline__ float2 seg_phase(const SegF *segf,
+                                            const float4 *pv, int n_seg,
+                                            int x, float hcr, double hconst) {
+    if constexpr (HT == HT_SEG) {
+        float hi = hcr, lo = 0.0f;
+        for (int s = 0; s < n_seg; ++s) {
+            float e;
+            hi = two_sum(hi, h_seg_f32(segf[s], __ldg(pv + s), x), e);
+            lo += e;
+        }
+        float sn, c;
+        __sincosf(reduce_2pi_ff(hi, lo), &sn, &c);
+        return make_float2(c, sn);
+    } else {
+        double acc = hconst;
+        for (int s = 0; s < n_seg; ++s)
+            acc += (double)h_seg_f32(segf[s], __ldg(pv + s), x);
+        return CS<float>::of_f64(acc);
+    }
+}
+
 // The march of one (row, angle group): row a.row0 + row_blk, deviation
 // parameters [grp * A, grp * A + A).  Every thread of the CTA calls it; the
 // CTA has 32 * WA * A threads or more (warps beyond WA * A idle).  smem: the
@@ -278,6 +321,20 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                 row[x] = R2{R(0), R(0)};
         }
     }
+    // Columns this thread evaluates the fused single-precision phase of:
+    // x = tid + i nthreads, i < nmine, all below Nx (CPL nthreads >= ncols
+    // bounds nmine by CPL).  The padding columns of both buffers are zeroed
+    // once here.
+    constexpr bool kFusedF32 = HT != HT_GENERIC && kSingle;
+    int nmine = 0;
+    if constexpr (kFusedF32) {
+        nmine = tid < Nx ? (Nx - 1 - tid) / nthreads + 1 : 0;
+        nmine = nmine < CPL ? nmine : CPL;
+        for (int x = Nx + tid; x < ncols; x += nthreads) {
+            cs[x] = R2{R(0), R(0)};
+            cs[ncols + x] = R2{R(0), R(0)};
+        }
+    }
     __syncthreads();
     // Sum over segments of the constant the single evaluator drops (double),
     // and that sum reduced mod 2 pi (start of the float-float sum).
@@ -309,8 +366,40 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         cp_async_commit();
     };
 
+    // Fused single precision: e^{iH(kk, x)} of this thread's columns into
+    // cs buffer `buf`.  One segment keeps its constants and pivot in
+    // registers across the columns; more segments sum in table order per
+    // column.  Both give the same bits for one segment.
+    auto produce_f32 = [&](int kk, int buf) {
+        R2 *dst = cs + (size_t)buf * ncols;
+        const float4 *pv = a.piv + ((size_t)row_blk * nsteps + kk) * a.n_seg;
+        if (a.n_seg == 1) {
+            const SegF f = segf[0];
+            const float4 p0 = __ldg(pv);
+#pragma unroll
+            for (int i = 0; i < CPL; ++i) {
+                if (i < nmine) {
+                    const int x = tid + i * nthreads;
+                    dst[x] = CS<R>::of_cs(seg_phase_one<HT>(f, p0, x, hcr, hconst));
+                }
+            }
+            return;
+        }
+#pragma unroll
+        for (int i = 0; i < CPL; ++i) {
+            if (i < nmine) {
+                const int x = tid + i * nthreads;
+                dst[x] = CS<R>::of_cs(
+                    seg_phase<HT>(segf, pv, a.n_seg, x, hcr, hconst));
+            }
+        }
+    };
+
     // e^{iH(kk, x)} of every padded column into cs buffer `buf`.
     auto produce = [&](int kk, int buf) {
+        if constexpr (kFusedF32) {
+            produce_f32(kk, buf);
+        } else {
         R2 *dst = cs + (size_t)buf * ncols;
         const unsigned char *st = raw + (size_t)(kk % 3) * plan.raw_stage;
 #pragma unroll
@@ -321,28 +410,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
             if (x >= Nx) {
                 v.x = R(0); v.y = R(0);
             } else if (HT != HT_GENERIC) {
-                if constexpr (kSingle) {
-                    const float4 *pv =
-                        a.piv + ((size_t)row_blk * nsteps + kk) * a.n_seg;
-                    if constexpr (HT == HT_SEG) {
-                        float hi = hcr, lo = 0.0f;
-                        for (int s = 0; s < a.n_seg; ++s) {
-                            float e;
-                            hi = two_sum(hi, h_seg_f32(segf[s], __ldg(pv + s), x),
-                                         e);
-                            lo += e;
-                        }
-                        float sn, c;
-                        __sincosf(reduce_2pi_ff(hi, lo), &sn, &c);
-                        v.x = c;
-                        v.y = sn;
-                    } else {
-                        double acc = hconst;
-                        for (int s = 0; s < a.n_seg; ++s)
-                            acc += (double)h_seg_f32(segf[s], __ldg(pv + s), x);
-                        v = CS<R>::of_f64(acc);
-                    }
-                } else {
+                if constexpr (!kSingle) {
                     const double X0 = __dmul_rn((double)x - 0.5 * Nx, a.dx);
                     const double yv = __dmul_rn((double)iy - 0.5 * a.Ny, a.dx);
                     const double zv = __dmul_rn((double)kk, a.dz);
@@ -400,6 +468,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                 }
             }
             dst[x] = v;
+        }
         }
     };
 
@@ -506,10 +575,11 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
             const R br = pbr, bi = pbi;
             pbr = Br[j]; pbi = Bi[j];
             const R2 e = src[j];
-            const R m12r = k12r * e.x - k12i * e.y;
-            const R m12i = k12r * e.y + k12i * e.x;
-            const R m21r = k21r * e.x + k21i * e.y;
-            const R m21i = k21i * e.x - k21r * e.y;
+            // Fixed rounding order (the packed pair march repeats it).
+            const R m12r = fmaR(k12r, e.x, -k12i * e.y);
+            const R m12i = fmaR(k12r, e.y, k12i * e.x);
+            const R m21r = fmaR(k21r, e.x, k21i * e.y);
+            const R m21i = fmaR(k21i, e.x, -k21r * e.y);
             if constexpr (!COMP) {
                 Ar[j] = fmaR(m12r, br, fmaR(-m12i, bi, ar));
                 Ai[j] = fmaR(m12r, bi, fmaR(m12i, br, ai));

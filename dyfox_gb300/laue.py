@@ -113,7 +113,7 @@ def _h_source_of(seg_list, xtal, H_gpu, pristine=False):
     return _lib.H_SEGMENTS
 
 
-def _flags(prec, h_mode, compensated, general, h_sum):
+def _flags(prec, h_mode, compensated, general, h_sum, pairs="auto"):
     if h_mode not in _MODES:
         raise ValueError(f"h_mode is one of {sorted(_MODES)}, not {h_mode!r}")
     flags = _MODES[h_mode]
@@ -125,13 +125,19 @@ def _flags(prec, h_mode, compensated, general, h_sum):
         raise ValueError(f"h_sum is 'ff' or 'fp64', not {h_sum!r}")
     if h_sum == "fp64":
         flags |= _lib.FLAG_H_FP64
+    if pairs not in ("auto", True, False):
+        raise ValueError(f"pairs is 'auto', True or False, not {pairs!r}")
+    if pairs is True:
+        flags |= _lib.FLAG_PAIRS
+    elif pairs is False:
+        flags |= _lib.FLAG_SCALAR
     return flags
 
 
 def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
            pristine, h_mode="auto", compensated=True, general=False,
            angles_per_cta=0, cols_per_lane=0, out=None, h_sum="ff",
-           tuned=True):
+           tuned=True, pairs="auto"):
     torch = _lib.torch_cuda()
     prec = as_precision(precision)
     s = np.atleast_1d(np.asarray(s_dev_arr, dtype=float))
@@ -139,7 +145,7 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
     _check_angles(s, xtal, geo)
     Nx, Ny, Nz = geo["Nx"], geo["Ny"], geo["Nz"]
     n_e = len(s)
-    flags = _flags(prec, h_mode, compensated, general, h_sum)
+    flags = _flags(prec, h_mode, compensated, general, h_sum, pairs)
     table_dev, n_seg, ap, H = None, 0, None, None
     h_source = _h_source_of(seg_list, xtal, H_gpu, pristine)
     if h_source in (_lib.H_GRID_F64, _lib.H_GRID_F32):
@@ -167,7 +173,9 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
             from .autotune import lookup
             shape = lookup(d)
             if shape is not None:
-                d.cols_per_lane, d.angles_per_cta = shape
+                d.cols_per_lane, d.angles_per_cta, use_pairs = shape
+                if pairs == "auto" and use_pairs:
+                    d.flags |= _lib.FLAG_PAIRS
         nbytes = _lib.lib().dyfox_laue_workspace_bytes(d)
         if nbytes == 0:
             _lib.check(_lib.DYFOX_EINVAL, "dyfox_laue_workspace_bytes")
@@ -180,7 +188,8 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
 
 
 def describe(seg_list, s_dev_arr, grid, xtal, *, H_gpu=None,
-             precision=FP64, h_mode="auto", compensated=True, h_sum="ff"):
+             precision=FP64, h_mode="auto", compensated=True, h_sum="ff",
+             pairs="auto"):
     """The C-ABI descriptor one solve_dislocation call would use (host only;
     the autotuner keys its cache on it)."""
     prec = as_precision(precision)
@@ -193,23 +202,26 @@ def describe(seg_list, s_dev_arr, grid, xtal, *, H_gpu=None,
     ap = analytic_line_params(seg_list, xtal) \
         if h_source == _lib.H_ANALYTIC else None
     return _desc(xtal, grid_arrays(grid), len(s), prec, h_source, n_seg, ap,
-                 _flags(prec, h_mode, compensated, False, h_sum))
+                 _flags(prec, h_mode, compensated, False, h_sum, pairs))
 
 
 def solve_dislocation(seg_list, s_dev_arr, grid, xtal, *, H_gpu=None,
                       batch=64, precision=FP64, h_mode="auto",
-                      compensated=True, h_sum="ff"):
+                      compensated=True, h_sum="ff", pairs="auto"):
     """Exit wave of a dislocation field at each deviation parameter.
 
     ``batch`` caps the angles per launch (results do not depend on it).
     Keyword-only extensions: ``h_mode`` ("auto", "fused": H evaluated inside
     the march, "staged": e^{iH} computed once into the workspace and read by
-    every angle group), ``compensated`` (FP32 two-sum updates, default on),
-    ``h_sum`` (FP32: segment sum and 2 pi reduction in float-float "ff",
-    default, or in double "fp64").
+    every angle group), ``compensated`` (FP32 compensated updates, default
+    on), ``h_sum`` (FP32: segment sum and 2 pi reduction in float-float
+    "ff", default, or in double "fp64"), ``pairs`` (FP32 compensated: march
+    two deviation parameters per thread in packed f32x2 arithmetic; "auto"
+    follows the autotuner and is the scalar march without a tuned shape;
+    the results are the same bits either way).
     """
     return _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
-                  False, h_mode, compensated, h_sum=h_sum)
+                  False, h_mode, compensated, h_sum=h_sum, pairs=pairs)
 
 
 def solve_pristine(s_dev_arr, grid, xtal, *, precision=FP64):

@@ -59,6 +59,12 @@ typedef enum dyfox_status {
 #define DYFOX_FLAG_H_FP64 16u  /* FP32 + H_SEGMENTS: sum the segment terms and
                                   reduce mod 2 pi in double instead of in
                                   float-float (two-sum) arithmetic           */
+#define DYFOX_FLAG_PAIRS 32u   /* FP32 compensated, fused segments or staged
+                                  e^{iH}, n_e >= 2: march two deviation
+                                  parameters per thread in packed f32x2
+                                  arithmetic (same results bit for bit)      */
+#define DYFOX_FLAG_SCALAR 64u  /* FP32: one deviation parameter per thread
+                                  (overrides DYFOX_FLAG_PAIRS)               */
 
 /* Doubles per entry of a segment table (dyfox_segment_table). */
 #define DYFOX_SEG_STRIDE 24

@@ -265,6 +265,32 @@ def test_fused_and_staged_phase_agree_bitwise(gpu, diamond400, small_grid,
     assert a.tobytes() == b.tobytes()
 
 
+@pytest.mark.parametrize("h_mode,h_sum", [("fused", "ff"),
+                                           ("fused", "fp64"),
+                                           ("staged", "ff")])
+@pytest.mark.parametrize("n_seg", [1, 4])
+def test_pair_march_agrees_with_scalar_march_bitwise(gpu, diamond400,
+                                                    small_grid, h_mode, h_sum,
+                                                    n_seg, rng):
+    """Two deviation parameters per thread in packed f32x2 arithmetic give
+    the scalar march's bits, at every pair shape, for even and odd angle
+    counts (the last pair of an odd count repeats its angle)."""
+    from dyfox_gb300.laue import _solve
+    segs = geometry_n(diamond400, small_grid) if n_seg == 1 else \
+        random_segments(diamond400, small_grid, n_seg, rng)
+    for n_e in (2, 5):
+        s = np.linspace(-3e5, 3e5, n_e)
+        ref = np_(_solve(segs, s, small_grid, diamond400, None, 0, "fp32",
+                         False, h_mode=h_mode, h_sum=h_sum, pairs=False,
+                         tuned=False))
+        for cpl, A in ((3, 2), (5, 4), (7, 6)):
+            got = np_(_solve(segs, s, small_grid, diamond400, None, 0,
+                             "fp32", False, h_mode=h_mode, h_sum=h_sum,
+                             pairs=True, cols_per_lane=cpl, angles_per_cta=A,
+                             tuned=False))
+            assert got.tobytes() == ref.tobytes(), (n_e, cpl, A)
+
+
 def test_general_march_agrees_with_register_march(gpu, diamond400,
                                                  small_grid):
     from dyfox_gb300.dislocations import compute_H_grid
@@ -392,7 +418,8 @@ def test_autotuner_caches_a_shape_that_changes_nothing(gpu, diamond400,
     assert len(r["candidates"]) >= 2
     assert (tmp_path / "tune.json").exists()
     d = describe(seg, s, small_grid, diamond400, precision="fp32")
-    assert autotune.lookup(d) == (r["cols_per_lane"], r["angles_per_cta"])
+    assert autotune.lookup(d) == (r["cols_per_lane"], r["angles_per_cta"],
+                                  r["pairs"])
     after = np_(solve_dislocation(seg, s, small_grid, diamond400,
                                   precision="fp32"))
     assert before.tobytes() == after.tobytes()
