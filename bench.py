@@ -59,11 +59,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--once", choices=["fp32", "fp64", "bragg", "bragg32",
-                                       "scan"],
+                                       "scan", "image"],
                     help="run one solve of that form after one warm-up and "
                          "exit (a small, fixed case for ncu)")
     ap.add_argument("--no-bragg", action="store_true")
     ap.add_argument("--no-scan", action="store_true")
+    ap.add_argument("--no-com-maps", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-train", type=int, default=16,
@@ -253,6 +254,18 @@ def run_ours(args):
                               h_mode="staged", batch=len(ss))
             torch.cuda.synchronize()
         return
+    if args.once == "image":
+        from dyfox_gb300.optics import Optics, image_intensity
+        from dyfox_gb300.workloads import laue_rocking_scan
+        sx, sgrid, ssegs, ss = laue_rocking_scan(n_angles=16)
+        stack = solve_dislocation(ssegs, ss, sgrid, sx, precision="fp32",
+                                  h_mode="staged", batch=len(ss))
+        lens = Optics(NA=1e-4, f_lens=0.274, xtal=sx, precision="fp32")
+        pup = lens.spiral(stack.shape[-1], stack.shape[-2], sgrid.dx, 2)
+        for _ in range(2):
+            image_intensity(stack, pup)
+            torch.cuda.synchronize()
+        return
     if args.once in ("bragg", "bragg32"):
         from dyfox_gb300.bragg import solve_scan
         bx, bcfg, bseg, bs, bys, bg = bragg_workload()
@@ -394,6 +407,8 @@ def run_ours(args):
         line["bragg"] = bragg_leg(args, rank, world)
     if not args.no_scan:
         line["laue_scan"] = scan_leg(args, world)
+    if not args.no_com_maps:
+        line["com_maps"] = com_maps_leg(args, world)
     if not args.no_batched:
         line["batched"] = batched_leg(args, world)
     if not args.no_learned:
@@ -796,6 +811,113 @@ def scan_leg(args, world):
             "intensity_rel_l2_vs_fp64_8_angles": err,
             "fp64_8_angles_s": fp64_s, "gpu_launches": int(launches),
             "launch_shape": shape}
+
+
+def hbm_peak():
+    """(GB/s, source) of the HBM copy rate measured on this machine, else the
+    fallback figure."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                        "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def com_maps_leg(args, world):
+    """Centre-of-mass maps (analysis.rocking.com_maps) of the 256-angle
+    rocking scan of the scan leg through spiral-plate charges 0 and 2 (NA
+    1e-4, f 0.274 m): the FP32 march of all angles in one call, the images
+    and the fused double-precision reduction, ending with the maps on the
+    host.  The imaging pass is also timed alone on resident exit waves (16
+    per launch, L2 flushed between launches) for its roofline: 8 bytes read
+    and 4 written per pixel.  Accuracy: maps from 16 of the angles against
+    the same maps in FP64, over the pixels holding 99% of the weight."""
+    import torch
+    from dyfox_gb300 import _lib
+    from dyfox_gb300.grid import grid_arrays
+    from dyfox_gb300.laue import solve_dislocation
+    from dyfox_gb300.optics import Optics, image_intensity
+    from dyfox_gb300.rocking import com_maps
+    from dyfox_gb300.workloads import laue_rocking_scan
+    x, grid, segs, s = laue_rocking_scan()
+    geo = grid_arrays(grid)
+    Ny, Nx = geo["Ny"], geo["Nx"]
+    ells = (0, 2)
+    lens = Optics(NA=1e-4, f_lens=0.274, xtal=x, precision="fp32")
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+
+    def run(ss, prec="fp32"):
+        return com_maps(segs, ss, grid, x, lens if prec == "fp32" else
+                        Optics(NA=1e-4, f_lens=0.274, xtal=x), ells,
+                        precision=prec, h_mode="staged")
+
+    run(s)
+    torch.cuda.synchronize()
+    times = []
+    n0 = L.dyfox_launch_count()
+    steps = max(3, args.steps // 8)
+    for _ in range(steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        run(s)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    launches = (L.dyfox_launch_count() - n0) // steps
+    ms = 1e3 * max_over_ranks(statistics.mean(times) * 1e-3, world)
+
+    # Imaging alone: 16 resident exit waves per launch through one pupil.
+    chunk = 16
+    stack = solve_dislocation(segs, s[:chunk], grid, x, precision="fp32",
+                              h_mode="staged", batch=chunk)
+    pup = lens.spiral(Nx, Ny, grid.dx, 2)
+    image_intensity(stack, pup)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    itimes = []
+    for _ in range(max(5, args.steps)):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        image_intensity(stack, pup)
+        b.record(stream)
+        torch.cuda.synchronize()
+        itimes.append(a.elapsed_time(b))
+    ims = statistics.median(itimes)
+    alg_bytes = chunk * Ny * Nx * (8 + 4)
+    peak, src = hbm_peak()
+    achieved = alg_bytes / (ims * 1e-3) / 1e9
+
+    # Accuracy on 16 angles: FP32 maps against FP64 maps.
+    pick = np.linspace(0, len(s) - 1, 16).round().astype(int)
+    c32, r32, w32 = run(s[pick])
+    c64, r64, w64 = run(s[pick], "fp64")
+    dev = {}
+    for e in ells:
+        w = w64[e].ravel()
+        order = np.argsort(w)[::-1]
+        keep = order[:np.searchsorted(np.cumsum(w[order]), 0.99 * w.sum()) + 1]
+        dev[str(e)] = float(np.abs(c32[e].ravel()[keep]
+                                   - c64[e].ravel()[keep]).max())
+    return {"value": world * len(s) / (ms * 1e-3), "unit": "scan angles/s",
+            "ms_per_scan": ms, "angles": len(s), "charges": list(ells),
+            "Ny": Ny, "Nx": Nx, "gpu_launches": int(launches),
+            "form": "FP32 march of all angles in one call (e^{iH} staged "
+                    "once), batched 2-D FFT imaging per charge, fused "
+                    "double-precision sums of phi I and I, maps to host",
+            "imaging": {"images_per_s": chunk / (ims * 1e-3),
+                        "ms_per_launch": ims, "images_per_launch": chunk,
+                        "roofline": {"bound": "hbm", "achieved": achieved,
+                                     "peak": peak, "unit": "GB/s",
+                                     "frac": achieved / peak,
+                                     "traffic": None,
+                                     "algorithmic_bytes_per_launch":
+                                         alg_bytes, "peak_source": src}},
+            "max_com_deviation_urad_vs_fp64_16_angles": dev}
 
 
 def bragg_leg(args, rank, world):

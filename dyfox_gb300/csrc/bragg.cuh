@@ -233,9 +233,18 @@ struct FftPlan {
     int n;
     int nfac;
     int fac[24];
+    // Per pass f: ceil(2^32 / Ns_f) and ceil(2^32 / (n / fac[f])), or 0
+    // where the divisor is 1.  __umulhi(i, magic) is then i / divisor,
+    // exactly for i < 2^16 and divisors below 2^16 (n <= 2^16).
+    unsigned ns_magic[24], nb_magic[24];
 };
 
+inline unsigned fft_magic(unsigned d) {
+    return d > 1 ? (unsigned)(((1ull << 32) + d - 1) / d) : 0u;
+}
+
 // Radices of an N-point transform: 4s, then 2s, then odd factors.
+// N <= 65536 (the magic divisions; callers check).
 inline FftPlan make_fft_plan(int N) {
     FftPlan p;
     memset(&p, 0, sizeof p);
@@ -245,6 +254,12 @@ inline FftPlan make_fft_plan(int N) {
     while (n % 2 == 0 && p.nfac < 24) { p.fac[p.nfac++] = 2; n /= 2; }
     for (int f = 3; n > 1 && p.nfac < 24; f += 2)
         while (n % f == 0 && p.nfac < 24) { p.fac[p.nfac++] = f; n /= f; }
+    unsigned Ns = 1;
+    for (int f = 0; f < p.nfac; ++f) {
+        p.ns_magic[f] = fft_magic(Ns);
+        p.nb_magic[f] = fft_magic((unsigned)(N / p.fac[f]));
+        Ns *= (unsigned)p.fac[f];
+    }
     return p;
 }
 
@@ -254,31 +269,112 @@ __device__ __forceinline__ C twid(const C *tw, int m, bool inv) {
     return inv ? cconj(w) : w;
 }
 
-// Returns the buffer holding the result (src or dst).  All threads call.
-// C is double2 or float2 (the table tw has the same type).
+__device__ __forceinline__ int fft_div(int i, unsigned magic) {
+    return magic ? (int)__umulhi((unsigned)i, magic) : i;
+}
+
+// One radix-R pass (R = 3, 5, 7) of `count` transforms: one thread per
+// butterfly.  Inputs are twiddled once, then the R-point DFT uses the
+// conjugate pairs r, R - r: with a_r = x_r + x_{R-r}, b_r = x_r - x_{R-r},
+// y_q = x_0 + sum a_r cos(2 pi r q / R) -+ i sum b_r sin(2 pi r q / R) and
+// y_{R-q} the other sign (forward / inverse), about half the products of
+// the plain sum.  cos and sin come from the N-point table at multiples of
+// N / R.
+template <int R, typename C>
+__device__ __forceinline__ void fft_odd_pass(const C *src, C *dst, int N,
+                                             int nb, int Ns, int step,
+                                             unsigned ns_mg, unsigned nb_mg,
+                                             int count, int stride,
+                                             const C *tw, bool inv) {
+    constexpr int H = (R - 1) / 2;
+    const int unit = N / R;
+    const int items = nb * count;
+    for (int t = threadIdx.x; t < items; t += blockDim.x) {
+        const int c = count > 1 ? fft_div(t, nb_mg) : 0;
+        const int j = t - c * nb;
+        const C *sc = src + (size_t)c * stride;
+        C *dc = dst + (size_t)c * stride;
+        const int q = fft_div(j, ns_mg), k = j - q * Ns;
+        C x[R];
+        x[0] = sc[j];
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            C v = sc[j + r * nb];
+            if (k) v = cmulz(v, twid(tw, r * k * step, inv));
+            x[r] = v;
+        }
+        C a[H], b[H];
+        C y0 = x[0];
+#pragma unroll
+        for (int r = 1; r <= H; ++r) {
+            a[r - 1] = cadd(x[r], x[R - r]);
+            b[r - 1] = csub(x[r], x[R - r]);
+            y0 = cadd(y0, a[r - 1]);
+        }
+        const int d = q * Ns * R + k;
+        dc[d] = y0;
+#pragma unroll
+        for (int qq = 1; qq <= H; ++qq) {
+            C P = x[0], Q;
+            Q.x = 0; Q.y = 0;
+#pragma unroll
+            for (int r = 1; r <= H; ++r) {
+                const C w = __ldg(tw + ((r * qq) % R) * unit);  // (cos, -sin)
+                P.x += a[r - 1].x * w.x;
+                P.y += a[r - 1].y * w.x;
+                Q.x -= b[r - 1].x * w.y;
+                Q.y -= b[r - 1].y * w.y;
+            }
+            // forward: y_qq = P - iQ, y_{R-qq} = P + iQ; inverse swaps.
+            C m, pl;
+            m.x = P.x + Q.y; m.y = P.y - Q.x;
+            pl.x = P.x - Q.y; pl.y = P.y + Q.x;
+            dc[d + qq * Ns] = inv ? pl : m;
+            dc[d + (R - qq) * Ns] = inv ? m : pl;
+        }
+    }
+}
+
+// Stockham FFT of `count` N-point transforms, transform c at offset
+// c * stride (stride >= N; 0: N), between two buffers.  Returns the buffer
+// holding the result (src or dst).  All threads call.  C is double2 or
+// float2 (the table tw has the same type).  count * (N / 2)^2 < 2^32 keeps
+// the magic division of the item index by N / R exact.
 template <typename C>
 __device__ C *fft_run(C *src, C *dst, const FftPlan &p,
-                      const C *__restrict__ tw, bool inv) {
+                                   const C *__restrict__ tw, bool inv,
+                                   int count = 1, int stride = 0) {
     const int N = p.n, tid = threadIdx.x, nt = blockDim.x;
+    if (stride == 0) stride = N;
     int Ns = 1;
     for (int f = 0; f < p.nfac; ++f) {
         const int R = p.fac[f];
         const int nb = N / R;
         const int step = N / (Ns * R);
+        const unsigned ns_mg = p.ns_magic[f], nb_mg = p.nb_magic[f];
+        const int items = nb * count;
         if (R == 2) {
-            for (int j = tid; j < nb; j += nt) {
-                const int k = j % Ns;
-                C a = src[j], b = src[j + nb];
+            for (int t = tid; t < items; t += nt) {
+                const int c = count > 1 ? fft_div(t, nb_mg) : 0;
+                const int j = t - c * nb;
+                const C *sc = src + (size_t)c * stride;
+                C *dc = dst + (size_t)c * stride;
+                const int q = fft_div(j, ns_mg), k = j - q * Ns;
+                C a = sc[j], b = sc[j + nb];
                 if (k) b = cmulz(b, twid(tw, k * step, inv));
-                const int d = (j / Ns) * Ns * 2 + k;
-                dst[d] = cadd(a, b);
-                dst[d + Ns] = csub(a, b);
+                const int d = q * Ns * 2 + k;
+                dc[d] = cadd(a, b);
+                dc[d + Ns] = csub(a, b);
             }
         } else if (R == 4) {
-            for (int j = tid; j < nb; j += nt) {
-                const int k = j % Ns;
-                C v0 = src[j], v1 = src[j + nb], v2 = src[j + 2 * nb],
-                  v3 = src[j + 3 * nb];
+            for (int t = tid; t < items; t += nt) {
+                const int c = count > 1 ? fft_div(t, nb_mg) : 0;
+                const int j = t - c * nb;
+                const C *sc = src + (size_t)c * stride;
+                C *dc = dst + (size_t)c * stride;
+                const int q = fft_div(j, ns_mg), k = j - q * Ns;
+                C v0 = sc[j], v1 = sc[j + nb], v2 = sc[j + 2 * nb],
+                  v3 = sc[j + 3 * nb];
                 if (k) {
                     v1 = cmulz(v1, twid(tw, k * step, inv));
                     v2 = cmulz(v2, twid(tw, 2 * k * step, inv));
@@ -290,27 +386,38 @@ __device__ C *fft_run(C *src, C *dst, const FftPlan &p,
                 C rot;
                 rot.x = inv ? -d13.y : d13.y;
                 rot.y = inv ? d13.x : -d13.x;
-                const int d = (j / Ns) * Ns * 4 + k;
-                dst[d] = cadd(s02, s13);
-                dst[d + Ns] = cadd(d02, rot);
-                dst[d + 2 * Ns] = csub(s02, s13);
-                dst[d + 3 * Ns] = csub(d02, rot);
+                const int d = q * Ns * 4 + k;
+                dc[d] = cadd(s02, s13);
+                dc[d + Ns] = cadd(d02, rot);
+                dc[d + 2 * Ns] = csub(s02, s13);
+                dc[d + 3 * Ns] = csub(d02, rot);
             }
+        } else if (R == 3) {
+            fft_odd_pass<3>(src, dst, N, nb, Ns, step, ns_mg, nb_mg, count, stride, tw, inv);
+        } else if (R == 5) {
+            fft_odd_pass<5>(src, dst, N, nb, Ns, step, ns_mg, nb_mg, count, stride, tw, inv);
+        } else if (R == 7) {
+            fft_odd_pass<7>(src, dst, N, nb, Ns, step, ns_mg, nb_mg, count, stride, tw, inv);
         } else {
-            for (int it = tid; it < N; it += nt) {
-                const int j = it % nb, q = it / nb;
-                const int k = j % Ns;
+            // Larger odd factors (11, 13, 17, 19, ...): one output per
+            // thread, the plain sum over the R inputs; few registers.
+            for (int it = tid; it < N * count; it += nt) {
+                const int c = count > 1 ? it / N : 0, o = it - c * N;
+                const C *sc = src + (size_t)c * stride;
+                C *dc = dst + (size_t)c * stride;
+                const int q = o / nb, j = o - q * nb;
+                const int jq = fft_div(j, ns_mg), k = j - jq * Ns;
                 // sum_r src[j + r nb] W^(r (k step + q nb))
                 int base = k * step + q * nb;
                 if (base >= N) base -= N;
-                C acc = src[j];
+                C acc = sc[j];
                 int m = base;
                 for (int r = 1; r < R; ++r) {
-                    acc = cadd(acc, cmulz(src[j + r * nb], twid(tw, m, inv)));
+                    acc = cadd(acc, cmulz(sc[j + r * nb], twid(tw, m, inv)));
                     m += base;
                     if (m >= N) m -= N;
                 }
-                dst[(j / Ns) * Ns * R + k + q * Ns] = acc;
+                dc[jq * Ns * R + k + q * Ns] = acc;
             }
         }
         __syncthreads();

@@ -96,39 +96,35 @@ __global__ void cols_pupil_kernel(C *data, int Ny, int Nx, int CB,
                                   FftPlan plan, const C *__restrict__ tw,
                                   const C *__restrict__ pupil) {
     extern __shared__ __align__(16) unsigned char smem[];
-    C *a = reinterpret_cast<C *>(smem), *b = a + (size_t)CB * Ny;
+    // Column c of the block at a[c * S + y]; S = Ny + 1 (odd) keeps the
+    // transposing loads and stores free of bank conflicts.
+    const int S = Ny + 1;
+    C *a = reinterpret_cast<C *>(smem), *b = a + (size_t)CB * S;
     const int nblk = (Nx + CB - 1) / CB;
     const int img = blockIdx.x / nblk, x0 = (blockIdx.x - img * nblk) * CB;
     const int nc = Nx - x0 < CB ? Nx - x0 : CB;
     C *base = data + (size_t)img * Ny * Nx;
     for (int t = threadIdx.x; t < Ny * CB; t += blockDim.x) {
         const int y = t / CB, c = t - y * CB;
-        if (c < nc) a[c * Ny + y] = base[(size_t)y * Nx + x0 + c];
+        if (c < nc) a[c * S + y] = base[(size_t)y * Nx + x0 + c];
     }
     __syncthreads();
-    C *res = a;
-    for (int c = 0; c < nc; ++c)
-        res = fft_run(a + (size_t)c * Ny, b + (size_t)c * Ny, plan, tw, false);
-    // every column's result sits in the same buffer (same plan)
-    res = res == a + (size_t)(nc - 1) * Ny ? a : b;
+    // The nc columns are transformed together (one barrier per pass).
+    C *res = fft_run(a, b, plan, tw, false, nc, S);
     for (int t = threadIdx.x; t < Ny * CB; t += blockDim.x) {
         const int y = t / CB, c = t - y * CB;
         if (c >= nc) continue;
         const int kx = x0 + c;
         const C p = __ldg(pupil + (size_t)((y + Ny / 2) % Ny) * Nx +
                           (kx + Nx / 2) % Nx);
-        res[c * Ny + y] = cmulz(res[c * Ny + y], p);
+        res[c * S + y] = cmulz(res[c * S + y], p);
     }
     __syncthreads();
     C *other = res == a ? b : a;
-    C *fin = res;
-    for (int c = 0; c < nc; ++c)
-        fin = fft_run(res + (size_t)c * Ny, other + (size_t)c * Ny, plan, tw,
-                      true);
-    fin = fin == res + (size_t)(nc - 1) * Ny ? res : other;
+    C *fin = fft_run(res, other, plan, tw, true, nc, S);
     for (int t = threadIdx.x; t < Ny * CB; t += blockDim.x) {
         const int y = t / CB, c = t - y * CB;
-        if (c < nc) base[(size_t)y * Nx + x0 + c] = fin[c * Ny + y];
+        if (c < nc) base[(size_t)y * Nx + x0 + c] = fin[c * S + y];
     }
 }
 
@@ -161,8 +157,9 @@ __global__ void rows_intensity_kernel(const C *__restrict__ data, int n,
         const C *r = fft_run(a, b, plan, tw, true);
         double part = 0.0;
         for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
-            const double vr = (double)r[x].x, vi = (double)r[x].y;
-            const R I = (R)((vr * vr + vi * vi) * scale);
+            // |.|^2 in the stack's precision, as the reference's abs()**2.
+            const R vr = r[x].x, vi = r[x].y;
+            const R I = (vr * vr + vi * vi) * (R)scale;
             if (img) img[row + x] = I;
             if (sum_I) {
                 const size_t p = (size_t)y * Nx + x;
@@ -224,10 +221,20 @@ static int image_plan(int n, int Ny, int Nx, int precision, ImagePlan *p) {
                                        cudaDevAttrMaxSharedMemoryPerBlockOptin,
                                        dev);
     if (e) return cuda_status(e, "device query");
+    if (Nx > 65536 || Ny > 65536) {
+        set_error("image of %d x %d: transforms are limited to 65536 points",
+                  Ny, Nx);
+        return DYFOX_EINVAL;
+    }
+    // Columns per block of the column pass: 8 where they fit in half the
+    // shared memory and keep the batched transform's index division exact
+    // (CB (Ny / 2)^2 < 2^32).
     p->CB = 8;
-    while (p->CB > 1 && 2 * (size_t)p->CB * Ny * cs > (size_t)optin / 2)
+    while (p->CB > 1 &&
+           (2 * (size_t)p->CB * (Ny + 1) * cs > (size_t)optin / 2 ||
+            (unsigned long long)p->CB * (Ny / 2) * (Ny / 2) >= (1ull << 32)))
         p->CB /= 2;
-    p->smem_cols = 2 * (size_t)p->CB * Ny * cs;
+    p->smem_cols = 2 * (size_t)p->CB * (Ny + 1) * cs;
     if (p->smem_cols > (size_t)optin || p->smem_last > (size_t)optin) {
         set_error("image of %d x %d needs more shared memory than the device "
                   "has", Ny, Nx);

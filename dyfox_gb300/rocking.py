@@ -8,11 +8,14 @@ centred on:
 
     COM(x, y) = sum_s phi(s) I(x, y, s) / sum_s I(x, y, s)
 
-with I the image through each pupil charge.  The exit waves of a batch go
-straight from the march into ``dyfox_image``, which images them and adds
-phi I and I into double-precision sums on the GPU; the scan is never held
-whole.  ``planewave_rocking`` is the closed-form perfect-crystal curve
-(analysis/rocking.py:16-34).
+with I the image through each pupil charge.  By default the whole scan is
+marched in one call (the e^{iH} field of the segments is then evaluated or
+staged once for all angles; a 256-angle complex64 scan of 544 x 1056 is
+1.2 GB), and the exit waves go in chunks of ``image_chunk`` straight into
+``dyfox_image``, which images them and adds phi I and I into
+double-precision sums on the GPU.  ``batch`` marches fewer angles at a time
+where memory is short, as the reference does.  ``planewave_rocking`` is the
+closed-form perfect-crystal curve (analysis/rocking.py:16-34).
 """
 
 import numpy as np
@@ -39,12 +42,14 @@ def planewave_rocking(s_dev, xtal, t_crystal, absorption=True):
 
 
 def com_maps(seg_list, s_dev_arr, grid, xtal, optics, ells=(0, 2), *,
-             batch=16, precision=FP64):
+             batch=None, precision=FP64, image_chunk=16, h_mode="auto"):
     """Centre-of-mass maps of a rocking scan, per pupil charge.
 
     Returns (com, rock, weight): dicts keyed by charge of the maps in
     microradians (Ny, Nx), the integrated rocking curve (n_s), and the
     summed intensity that weighted the maps (Ny, Nx), all NumPy.
+    ``batch``: angles per march call (None: all); ``image_chunk``: exit
+    waves per imaging launch (their intermediate spectra stay in L2).
     """
     torch = _lib.torch_cuda()
     s = np.asarray(s_dev_arr, dtype=float)
@@ -55,16 +60,22 @@ def com_maps(seg_list, s_dev_arr, grid, xtal, optics, ells=(0, 2), *,
     sums_I = {e: torch.zeros((Ny, Nx), dtype=torch.float64, device="cuda")
               for e in ells}
     rock = {e: np.zeros(len(s)) for e in ells}
+    batch = len(s) if not batch else int(batch)
+    chunk = max(1, int(image_chunk))
     for bs in range(0, len(s), batch):
         be = min(bs + batch, len(s))
         stack = solve_dislocation(seg_list, s[bs:be], grid, xtal,
-                                  precision=precision)
+                                  precision=precision, h_mode=h_mode,
+                                  batch=be - bs)
         for e in ells:
             pup = optics.spiral(Nx, Ny, grid.dx, e)
             if pup.dtype != stack.dtype:
                 pup = pup.to(stack.dtype)
-            rock[e][bs:be] = accumulate_com(stack, pup, phi[bs:be],
-                                            sums_wI[e], sums_I[e])
+            for cs in range(0, be - bs, chunk):
+                ce = min(cs + chunk, be - bs)
+                rock[e][bs + cs:bs + ce] = accumulate_com(
+                    stack[cs:ce], pup, phi[bs + cs:bs + ce], sums_wI[e],
+                    sums_I[e])
         del stack
     com = {e: (sums_wI[e] / torch.clamp(sums_I[e], min=1e-300)).cpu().numpy()
            for e in ells}

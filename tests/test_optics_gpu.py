@@ -73,10 +73,11 @@ def test_com_reduction(gpu, og):
     assert rel_l2(rock, want_I.sum(axis=(1, 2))) < 1e-12
 
 
-def test_com_maps_end_to_end(gpu, diamond400, small_grid):
-    """com_maps over a small scan (batches of 3 angles) equals the same
-    reduction written out over the whole stack with the library's own solve
-    and imaging calls."""
+@pytest.mark.parametrize("batch,chunk", [(3, 16), (None, 2)])
+def test_com_maps_end_to_end(gpu, diamond400, small_grid, batch, chunk):
+    """com_maps over a small scan (in march batches of 3 angles, or all at
+    once imaged 2 at a time) equals the same reduction written out over the
+    whole stack with the library's own solve and imaging calls."""
     from dyfox_gb300.laue import solve_dislocation
     from dyfox_gb300.optics import Optics, image_intensity
     from dyfox_gb300.rocking import com_maps
@@ -89,7 +90,7 @@ def test_com_maps_end_to_end(gpu, diamond400, small_grid):
     seg = [(np.array([-200e-6, 0.3e-6, 10e-6]),
             np.array([200e-6, 0.3e-6, 10e-6]), b)]
     com, rock, weight = com_maps(seg, s, grid, diamond400, lens,
-                                 ells=(0, 2), batch=3)
+                                 ells=(0, 2), batch=batch, image_chunk=chunk)
     phi = urad_from_deviation(s, diamond400)
     stack = solve_dislocation(seg, s, grid, diamond400)
     for ell in (0, 2):
