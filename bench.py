@@ -75,6 +75,12 @@ def parse():
     ap.add_argument("--learned-tmax", type=float, default=25e-6,
                     help="thickest instance of the learned-guess leg (m); "
                          "the configuration's range ends at 100e-6")
+    ap.add_argument("--batched-h-sum", choices=["ff", "fp64"],
+                    default="fp64",
+                    help="H segment sum of the batched leg's Laue instances: "
+                         "IEEE double (the chosen form: its worst instance "
+                         "stays within the 1e-5 budget) or float-float "
+                         "(FP64-class, faster); the other is timed beside it")
     ap.add_argument("--batched-sample", type=int, default=0,
                     help="batched leg on the first N instances (0: all 512)")
     ap.add_argument("--no-tune", action="store_true",
@@ -471,9 +477,11 @@ def _fp64_row_checks(W, outs, n_streams=16):
 def batched_leg(args, world):
     """Batched uneven instances: 512 seeded instances (70% Laue, 30% Bragg),
     one CUDA graph per replay (per-instance set-up, one persistent Laue
-    march launch, one Bragg launch).  Laue: compensated FP32 march with the
-    segment sum and 2 pi reduction in double (complex64 state, FP64 H);
-    Bragg: mixed-precision solve to true residual 1e-10.  Launch shape
+    march launch, one Bragg launch).  Laue: compensated FP32 march
+    (complex64 state) with an FP64-class H: the segment sum and 2 pi
+    reduction in IEEE double (``--batched-h-sum fp64``, the chosen form) or
+    in float-float (``ff``); the Laue part is timed alone in both.  Bragg:
+    mixed-precision solve to true residual 1e-10.  Launch shape
     from the batch autotuner.  Per-instance error against plain FP64 (Laue:
     central row at the first and last angle; Bragg: every system); a
     sample of the instances is also timed as plain FP64 single calls and as
@@ -486,6 +494,7 @@ def batched_leg(args, world):
     from dyfox_gb300.laue import solve_dislocation
     from dyfox_gb300.workloads import batched_uneven
     L = _lib.lib()
+    hs = args.batched_h_sum
     W = batched_uneven()
     if args.batched_sample:
         W = W[:args.batched_sample]
@@ -494,11 +503,11 @@ def batched_leg(args, world):
     if args.no_tune:
         tuned = {"cols_per_lane": 5, "warps": 8, "ms": None}
     else:
-        tuned = autotune(inst, h_sum="fp64")
+        tuned = autotune(inst, h_sum=hs)
     tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     b = Batch(inst, cols_per_lane=tuned["cols_per_lane"],
-              warps=tuned["warps"], h_sum="fp64")
+              warps=tuned["warps"], h_sum=hs)
     plan_s = time.perf_counter() - t0
     for _ in range(2):
         b.run()
@@ -530,12 +539,14 @@ def batched_leg(args, world):
     bi = [i for i, w in enumerate(W) if w["kind"] == "bragg"]
     # the two parts alone (each its own graph)
     part_ms = {}
-    for key, idx in (("laue", li), ("bragg", bi)):
+    other = "fp64" if hs == "ff" else "ff"
+    for key, idx, h in (("laue", li, hs), ("bragg", bi, hs),
+                        ("laue_" + other, li, other)):
         if not idx:
             continue
         pb = Batch([inst[i] for i in idx],
                    cols_per_lane=tuned["cols_per_lane"],
-                   warps=tuned["warps"], h_sum="fp64")
+                   warps=tuned["warps"], h_sum=h)
         pb.run()
         torch.cuda.synchronize()
         a0 = torch.cuda.Event(enable_timing=True)
@@ -564,7 +575,7 @@ def batched_leg(args, world):
     # a sample as single calls: plain FP64 and FP32
     samp = li[:12] + bi[:6]
     sub = Batch([inst[i] for i in samp], cols_per_lane=tuned["cols_per_lane"],
-                warps=tuned["warps"], h_sum="fp64")
+                warps=tuned["warps"], h_sum=hs)
     sub.run()
     torch.cuda.synchronize()
 
@@ -581,7 +592,7 @@ def batched_leg(args, world):
             if w["kind"] == "laue":
                 solve_dislocation(w["segs"], w["s"], w["grid"], w["xtal"],
                                   precision=prec,
-                                  h_sum="fp64" if prec == "fp32" else "ff")
+                                  h_sum=hs if prec == "fp32" else "ff")
             else:
                 solve_scan(w["segs"], w["s"], w["cfg"], w["ys"], w["xtal"],
                            w["g"], precision=prec)
@@ -598,15 +609,22 @@ def batched_leg(args, world):
             "ms": part_ms.get("laue"),
             "voxel_steps_per_s": world * laue_vs / (part_ms["laue"] * 1e-3)
             if "laue" in part_ms else None},
+        "laue_part_alone_h_sum_" + other: {
+            "ms": part_ms.get("laue_" + other),
+            "voxel_steps_per_s":
+                world * laue_vs / (part_ms["laue_" + other] * 1e-3)
+                if "laue_" + other in part_ms else None},
         "bragg_part_alone": {
             "ms": part_ms.get("bragg"),
             "solves_per_s": world * bragg_solves / (part_ms["bragg"] * 1e-3)
             if "bragg" in part_ms else None},
         "form": "one CUDA graph per replay: per-instance set-up, one "
                 "persistent Laue march launch (compensated FP32, segment sum "
-                "and 2 pi reduction in double, e^{iH} of each row evaluated "
-                "once by the CTA that marches it), one mixed-precision Bragg "
-                "launch",
+                "and 2 pi reduction " + ("in float-float, FP64-class"
+                                         if hs == "ff" else "in double") +
+                ", e^{iH} of each row evaluated once by the CTA that "
+                "marches it), one mixed-precision Bragg launch",
+        "h_sum": hs,
         "launch_shape": {"cols_per_lane": tuned["cols_per_lane"],
                          "warps": tuned["warps"], "tuner_ms": tuned["ms"],
                          "tuner_s": tune_s},
