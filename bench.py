@@ -941,10 +941,10 @@ def com_maps_leg(args, world):
 def bragg_leg(args, rank, world):
     """Bragg solves/s of config 1: all 21 deviation parameters x 64 planes
     in one batched launch (one solve = one deviation parameter over all
-    planes, to true relative residual <= 1e-10 computed in double).  The
-    chosen form is the mixed-precision solve (single-precision Krylov
-    products, double residuals and solution); plain FP64 is timed beside
-    it, and the two answers are compared."""
+    planes, to true relative residual <= 1e-10).  The chosen form is the
+    mixed-precision solve (single-precision Krylov products, float-float
+    right-hand side and true residuals, double Gram-Schmidt and solution);
+    plain FP64 is timed beside it, and the two answers are compared."""
     import torch
     from dyfox_gb300 import _lib
     from dyfox_gb300.bragg import solve_scan
@@ -982,9 +982,9 @@ def bragg_leg(args, rank, world):
            "ms_per_scan": ms, "solves_per_scan": len(s),
            "planes": len(ys), "Nx": cfg.Nx, "Nz": cfg.Nz,
            "form": "mixed precision: FP32 march + FFT preconditioner in the "
-                   "Arnoldi products, FP64 right-hand side, true residuals, "
-                   "Gram-Schmidt, rotations and solution; per-plane "
-                   "GMRES(40), one launch per scan",
+                   "Arnoldi products, float-float (FP64-class) right-hand "
+                   "side and true residuals, FP64 Gram-Schmidt, rotations "
+                   "and solution; per-plane GMRES(40), one launch per scan",
            "max_true_residual": float(inf[:, 0].max()),
            "max_inner_iterations": int(inf[:, 1].max()),
            "converged": bool((inf[:, 0] <= 1e-10).all()),

@@ -12,11 +12,12 @@
 // v e^{-iH(z=0)}.
 //
 // Precision DYFOX_FP32 is a mixed-precision form of the same solve: the
-// Arnoldi products (march and preconditioner) run in single precision
-// while b, every true residual, the Gram-Schmidt coefficients, the Givens
-// rotations and the solution stay in double.  Each restart is then one step
-// of iterative refinement on the double residual, so the solve still stops
-// at true relative residual <= tol computed in double; a restart cycle
+// Arnoldi products (march and preconditioner) run in single precision, b
+// and every true residual come from a float-float march (FP64-class, at a
+// fraction of the double pipe's time), and the Gram-Schmidt coefficients,
+// the Givens rotations and the solution stay in double.  Each restart is
+// then one step of iterative refinement on that residual, so the solve
+// still stops at true relative residual <= tol; a restart cycle
 // stops its inner iteration once the estimated residual has dropped by
 // kMixedInnerDrop, below which the single-precision operator's own error
 // makes further inner steps useless.  A system the mixed solve does not
@@ -36,7 +37,8 @@ namespace dyfox {
 // Couplings of every plane: cb = ds (sigma_hbar e^{+iH}), ch = ds (sigma_h
 // e^{-iH}) with H the Volterra phase at (x_i, y_p, z_k) summed in segment
 // order; e0h = e^{-iH} at k = 0.  One thread per voxel.
-// cb32, ch32 (may be NULL): the same couplings rounded to float.
+// cb32, ch32 (may be NULL): the same couplings rounded to float; cbl32,
+// chl32: the remainders, rounded to float (float-float couplings).
 __global__ void bragg_couple_kernel(const double *__restrict__ segs,
                                     int n_seg, int Nx, int Nz, double dx,
                                     double dz, VolterraConsts vc,
@@ -44,7 +46,8 @@ __global__ void bragg_couple_kernel(const double *__restrict__ segs,
                                     double ds, double shr, double shi,
                                     double sbr, double sbi, double2 *cb,
                                     double2 *ch, double2 *e0h, float2 *cb32,
-                                    float2 *ch32) {
+                                    float2 *ch32, float2 *cbl32,
+                                    float2 *chl32) {
     const long total = (long)n_y * Nz * Nx;
     for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total;
          idx += (long)gridDim.x * blockDim.x) {
@@ -71,8 +74,14 @@ __global__ void bragg_couple_kernel(const double *__restrict__ segs,
         cb[idx] = vb;
         ch[idx] = vh;
         if (cb32) {
-            cb32[idx] = make_float2((float)vb.x, (float)vb.y);
-            ch32[idx] = make_float2((float)vh.x, (float)vh.y);
+            const float2 b32 = make_float2((float)vb.x, (float)vb.y);
+            const float2 h32 = make_float2((float)vh.x, (float)vh.y);
+            cb32[idx] = b32;
+            ch32[idx] = h32;
+            cbl32[idx] = make_float2((float)(vb.x - (double)b32.x),
+                                     (float)(vb.y - (double)b32.y));
+            chl32[idx] = make_float2((float)(vh.x - (double)h32.x),
+                                     (float)(vh.y - (double)h32.y));
         }
         if (k == 0) e0h[(size_t)p * Nx + x] = make_double2(c, -sn);
     }
@@ -153,7 +162,7 @@ struct BraggPlan {
     int threads, cpl;
     bool mixed;
     size_t off_cb, off_ch, off_e0h, off_inc, off_iT, off_tw, off_y;
-    size_t off_cb32, off_ch32, off_iT32, off_tw32;
+    size_t off_cb32, off_ch32, off_cbl32, off_chl32, off_iT32, off_tw32;
     size_t off_V, off_H, off_X, off_B, off_info, ws;
 };
 
@@ -215,6 +224,8 @@ static int bragg_plan(const dyfox_bragg_desc *d, BraggPlan *p) {
     const size_t plane32 = (size_t)d->Nz * Nx * sizeof(float2) * f32;
     p->off_cb32 = o; o = a256(o + d->n_y * plane32);
     p->off_ch32 = o; o = a256(o + d->n_y * plane32);
+    p->off_cbl32 = o; o = a256(o + d->n_y * plane32);
+    p->off_chl32 = o; o = a256(o + d->n_y * plane32);
     p->off_iT32 = o; o = a256(o + f32 * d->n_s * Nx * sizeof(float2));
     p->off_tw32 = o; o = a256(o + f32 * Nx * sizeof(float2));
     p->off_V = o; o = a256(o + nsys * (m + 1) * Nx * sizeof(double2));
@@ -261,6 +272,8 @@ static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
     if (p.mixed) {
         a->cb32 = (const float2 *)(ws + p.off_cb32);
         a->ch32 = (const float2 *)(ws + p.off_ch32);
+        a->cbl32 = (const float2 *)(ws + p.off_cbl32);
+        a->chl32 = (const float2 *)(ws + p.off_chl32);
         a->iT32 = (const float2 *)(ws + p.off_iT32);
         a->tw32 = (const float2 *)(ws + p.off_tw32);
     }
@@ -290,7 +303,8 @@ static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
         seg_table, d->n_seg, d->Nx, d->Nz, d->dx, d->dz,
         volterra_consts(d->nu, d->a_core), y, d->n_y, d->ds, a->shr, a->shi,
         a->sbr, a->sbi, (double2 *)a->cb, (double2 *)a->ch, (double2 *)a->e0h,
-        (float2 *)a->cb32, (float2 *)a->ch32);
+        (float2 *)a->cb32, (float2 *)a->ch32, (float2 *)a->cbl32,
+        (float2 *)a->chl32);
     incident_kernel<<<div_up(d->Nx, 256), 256, 0, stream>>>(
         (double2 *)a->inc, d->Nx, d->dx, d->beam, d->beam_thickness,
         d->beam_centre);

@@ -222,6 +222,118 @@ __device__ void bragg_march32(const float2 *__restrict__ cb,
 }
 
 // ---------------------------------------------------------------------------
+// Float-float ("double-single") complex arithmetic, for the right-hand side
+// and the true residuals of the mixed-precision solve.  A real number is
+// hi + lo (|lo| <= ulp(hi) / 2); a complex number is the float4 (re.hi,
+// re.lo, im.hi, im.lo).  Products are Dekker's (the FMA residual of the
+// high parts) with the first-order cross terms, sums Knuth's two-sum:
+// relative error about 2^-44 a step, against 2^-53 in double, at several
+// times less pipe time on a part whose double rate is 1/64 of single.
+// __fmul_rn / __fadd_rn keep the compiler from contracting the products
+// whose rounding error is being captured.
+__device__ __forceinline__ float2 ff_of(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ float4 ffc_of(double2 v) {
+    const float2 r = ff_of(v.x), i = ff_of(v.y);
+    return make_float4(r.x, r.y, i.x, i.y);
+}
+__device__ __forceinline__ double2 ffc_to(float4 v) {
+    return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+}
+
+// c + a1 b1 + a2 b2, real float-float.
+__device__ __forceinline__ float2 ff_dot2(float2 a1, float2 b1, float2 a2,
+                                          float2 b2, float2 c) {
+    const float p1 = __fmul_rn(a1.x, b1.x), p2 = __fmul_rn(a2.x, b2.x);
+    float e = __fadd_rn(fmaf(a1.x, b1.x, -p1), fmaf(a2.x, b2.x, -p2));
+    e = fmaf(a1.x, b1.y, e);
+    e = fmaf(a1.y, b1.x, e);
+    e = fmaf(a2.x, b2.y, e);
+    e = fmaf(a2.y, b2.x, e);
+    float s = __fadd_rn(c.x, p1);
+    float v = __fsub_rn(s, c.x);
+    e = __fadd_rn(e, __fadd_rn(__fsub_rn(c.x, __fsub_rn(s, v)), __fsub_rn(p1, v)));
+    const float s2 = __fadd_rn(s, p2);
+    v = __fsub_rn(s2, s);
+    e = __fadd_rn(e, __fadd_rn(__fsub_rn(s, __fsub_rn(s2, v)), __fsub_rn(p2, v)));
+    e = __fadd_rn(e, c.y);
+    const float t = __fadd_rn(s2, e);
+    return make_float2(t, __fsub_rn(e, __fsub_rn(t, s2)));
+}
+
+// c + a b, complex float-float.
+__device__ __forceinline__ float4 ffc_fma(float4 a, float4 b, float4 c) {
+    const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
+    const float2 br = make_float2(b.x, b.y), bi = make_float2(b.z, b.w);
+    const float2 re = ff_dot2(ar, br, make_float2(-a.z, -a.w), bi,
+                              make_float2(c.x, c.y));
+    const float2 im = ff_dot2(ar, bi, ai, br, make_float2(c.z, c.w));
+    return make_float4(re.x, re.y, im.x, im.y);
+}
+
+// The down-march of bragg_march in float-float: couplings as hi (cb, ch)
+// and lo (cbl, chl) float2 planes, step factors e0, ieg as float-float,
+// inputs (NULL: zero) and the result in double.  ex0, ex1: float4 exchange
+// rows of Nx.
+template <int CPL>
+__device__ void bragg_march_ff(const float2 *__restrict__ cb,
+                               const float2 *__restrict__ cbl,
+                               const float2 *__restrict__ ch,
+                               const float2 *__restrict__ chl, float4 e0,
+                               float4 ieg, int Nz, int Nx,
+                               const double2 *d0_in, const double2 *dg_in,
+                               float4 *ex0, float4 *ex1, double2 *out) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 D0[CPL], Dg[CPL];
+#pragma unroll
+    for (int i = 0; i < CPL; ++i) {
+        const int x = tid + i * nt;
+        D0[i] = z4;
+        Dg[i] = z4;
+        if (x < Nx) {
+            if (d0_in) D0[i] = ffc_of(d0_in[x]);
+            if (dg_in) Dg[i] = ffc_of(dg_in[x]);
+        }
+    }
+    for (int k = 0; k < Nz - 1; ++k) {
+        const size_t row = (size_t)k * Nx;
+#pragma unroll
+        for (int i = 0; i < CPL; ++i) {
+            const int x = tid + i * nt;
+            if (x < Nx) {
+                const float2 bh = __ldg(cb + row + x), bl = __ldg(cbl + row + x);
+                const float2 hh = __ldg(ch + row + x), hl = __ldg(chl + row + x);
+                const float4 b = make_float4(bh.x, bl.x, bh.y, bl.y);
+                const float4 nh = make_float4(-hh.x, -hl.x, -hh.y, -hl.y);
+                const float4 u = ffc_fma(b, Dg[i], D0[i]);
+                const float4 w = ffc_fma(nh, D0[i], Dg[i]);
+                ex0[x + 1 == Nx ? 0 : x + 1] = ffc_fma(e0, u, z4);
+                ex1[x == 0 ? Nx - 1 : x - 1] = ffc_fma(w, ieg, z4);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < CPL; ++i) {
+            const int x = tid + i * nt;
+            if (x < Nx) {
+                D0[i] = ex0[x];
+                Dg[i] = ex1[x];
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < CPL; ++i) {
+        const int x = tid + i * nt;
+        if (x < Nx) out[x] = ffc_to(Dg[i]);
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
 // Mixed-radix Stockham FFT (Govindaraju et al., SC'08 formulation): stage of
 // radix R over butterflies j in [0, N/R), Ns = product of earlier radices;
 // input index j + r N/R, output index (j / Ns) Ns R + j % Ns + q Ns.  The
@@ -481,6 +593,8 @@ struct BraggArgs {
     const double2 *iT;            // (n_s, Nx): 1 / T22s
     const double2 *tw;            // (Nx): exp(-2 pi i m / Nx)
     const float2 *cb32, *ch32;    // FP32 copies of cb, ch (mixed form)
+    const float2 *cbl32, *chl32;  // cb - cb32, ch - ch32 rounded to float:
+                                  // the float-float couplings (mixed form)
     const float2 *iT32, *tw32;    // FP32 copies of iT, tw (mixed form)
     FftPlan plan;
     double2 *V;                   // (n_sys, m + 1, Nx)

@@ -90,6 +90,9 @@ __device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
     const float2 iegf = make_float2((float)ieg.x, (float)ieg.y);
     const float2 *cb32 = MIXED ? a.cb32 + (size_t)iy * a.Nz * Nx : nullptr;
     const float2 *ch32 = MIXED ? a.ch32 + (size_t)iy * a.Nz * Nx : nullptr;
+    const float2 *cbl32 = MIXED ? a.cbl32 + (size_t)iy * a.Nz * Nx : nullptr;
+    const float2 *chl32 = MIXED ? a.chl32 + (size_t)iy * a.Nz * Nx : nullptr;
+    const float4 e0ff = ffc_of(e0), iegff = ffc_of(ieg);
     const float2 *iT32 = MIXED ? a.iT32 + (size_t)is * Nx : nullptr;
     const double eps = 2.220446049250313e-16;
 
@@ -98,12 +101,21 @@ __device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
         for (int x = tid; x < Nx; x += nt) t.x += cabs2(v[x]);
         return sqrt(block_sum(t, red).x);
     };
-    // W <- A src (src NULL: particular solution from the incident beam)
+    // W <- A src (src NULL: particular solution from the incident beam); in
+    // float-float when MIXED (the right-hand side and the true residuals).
     auto matvec = [&](const double2 *src) {
-        if (src) bragg_march<CPL>(cb, ch, e0, ieg, a.Nz, Nx, nullptr, src,
-                                  A0, A1, W);
-        else bragg_march<CPL>(cb, ch, e0, ieg, a.Nz, Nx, a.inc, nullptr, A0,
-                              A1, W);
+        if (MIXED) {
+            bragg_march_ff<CPL>(cb32, cbl32, ch32, chl32, e0ff, iegff, a.Nz,
+                                Nx, src ? nullptr : a.inc, src,
+                                reinterpret_cast<float4 *>(A0),
+                                reinterpret_cast<float4 *>(A1), W);
+        } else if (src) {
+            bragg_march<CPL>(cb, ch, e0, ieg, a.Nz, Nx, nullptr, src, A0, A1,
+                             W);
+        } else {
+            bragg_march<CPL>(cb, ch, e0, ieg, a.Nz, Nx, a.inc, nullptr, A0,
+                             A1, W);
+        }
     };
     // The Arnoldi operator: W <- M A src, in single precision when MIXED.
     auto inner_op = [&](const double2 *src) {

@@ -195,11 +195,12 @@ size_t dyfox_bragg_workspace_bytes(const dyfox_bragg_desc *d);
  * doubles per system: true relative residual, inner iterations, code (0
  * converged, else maxiter), |b|; or NULL.
  * precision DYFOX_FP32: mixed-precision solve.  The Arnoldi products (march
- * and preconditioner) run in single precision; b, every true residual, the
- * Gram-Schmidt coefficients, the rotations and the solution stay in double,
- * so the stopping test is the same double-precision true residual <= tol.
- * Inputs and outputs keep their complex128 layout.  The workspace grows by
- * the single-precision couplings. */
+ * and preconditioner) run in single precision; b and every true residual
+ * come from a float-float march (about 2^-44 relative a step); the
+ * Gram-Schmidt coefficients, the rotations and the solution stay in
+ * double, so the stopping test is the same true residual <= tol.  Inputs
+ * and outputs keep their complex128 layout.  The workspace grows by the
+ * single-precision couplings and their remainders. */
 int dyfox_bragg_solve(const dyfox_bragg_desc *d, const double *seg_table,
                       const double *y_values, const double *s_dev,
                       const void *x0, void *out, double *info,
