@@ -238,7 +238,11 @@ def apply_operator(seg_list, s_values, cfg, y_values, xtal, g_vec, mode,
     """The down-march (mode "march": D_g(t) of (D0(0), Dg(0)) = (in0, in1))
     or the preconditioner (mode "precond": M in0) for every (s, plane);
     inputs and output are (n_s, n_y, Nx) complex128 CUDA tensors.
-    precision=FP32: the single-precision operators of the mixed solve."""
+    precision=FP32: the single-precision operators of the mixed solve, and
+    mode "march_ff": its float-float march (right-hand side, residuals)."""
+    modes = {"march": 0, "precond": 1, "march_ff": 2}
+    if mode not in modes:
+        raise ValueError(f"mode is one of {sorted(modes)}, not {mode!r}")
     prob = _Problem(seg_list, s_values, cfg, y_values, xtal, g_vec,
                     precision)
     torch = prob.torch
@@ -247,7 +251,7 @@ def apply_operator(seg_list, s_values, cfg, y_values, xtal, g_vec, mode,
     out = torch.empty((len(prob.s), len(prob.y), int(cfg.Nx)),
                       dtype=torch.complex128, device="cuda")
     _lib.check(_L().dyfox_bragg_apply(
-        d, 0 if mode == "march" else 1, _lib.ptr(prob.table), _yp(prob),
+        d, modes[mode], _lib.ptr(prob.table), _yp(prob),
         _lib.ptr(prob.s_dev), _lib.ptr(in0), _lib.ptr(in1), _lib.ptr(out),
         _lib.ptr(ws), ws.numel(), _lib.stream_ptr()), "dyfox_bragg_apply")
     return out

@@ -449,8 +449,9 @@ extern "C" int dyfox_bragg_apply(const dyfox_bragg_desc *d, int mode,
     BraggPlan p;
     int st = bragg_plan(d, &p);
     if (st) return st;
-    if (mode != 0 && mode != 1) {
-        set_error("mode is 0 (march) or 1 (preconditioner)");
+    if (mode < 0 || mode > 2 || (mode == 2 && !p.mixed)) {
+        set_error("mode is 0 (march), 1 (preconditioner) or, with precision "
+                  "DYFOX_FP32, 2 (float-float march)");
         return DYFOX_EINVAL;
     }
     if (!y_values || !s_dev || !out || (mode == 1 && !in0) ||

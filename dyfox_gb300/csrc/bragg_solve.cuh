@@ -382,7 +382,21 @@ __global__ void bragg_apply_kernel(const BraggArgs a, int mode,
     double2 *W = A1 + Nx;
     const int sys = blockIdx.x, is = sys / a.n_y, iy = sys - is * a.n_y;
     const size_t off = (size_t)sys * Nx;
-    if (mode == 0) {
+    if (mode == 2) {
+        // the float-float march of the mixed form's residuals
+        double2 e0, ieg;
+        step_factors(a, is, e0, ieg);
+        if (MIXED)
+            bragg_march_ff<CPL>(a.cb32 + (size_t)iy * a.Nz * Nx,
+                                a.cbl32 + (size_t)iy * a.Nz * Nx,
+                                a.ch32 + (size_t)iy * a.Nz * Nx,
+                                a.chl32 + (size_t)iy * a.Nz * Nx,
+                                ffc_of(e0), ffc_of(ieg), a.Nz, Nx,
+                                d0 ? d0 + off : nullptr,
+                                dg ? dg + off : nullptr,
+                                reinterpret_cast<float4 *>(A0),
+                                reinterpret_cast<float4 *>(A1), W);
+    } else if (mode == 0) {
         double2 e0, ieg;
         step_factors(a, is, e0, ieg);
         if (MIXED)

@@ -209,7 +209,9 @@ int dyfox_bragg_solve(const dyfox_bragg_desc *d, const double *seg_table,
 /* One operator application per system, for parity checks.
  * mode 0: out = down-march of (D0(0), Dg(0)) = (in0, in1) to D_g(t)
  *         (bragg/solver.py:28-35; NULL input = zero);
- * mode 1: out = ifft(fft(in0) / T22s) (solver.py:167-168, 297-300).
+ * mode 1: out = ifft(fft(in0) / T22s) (solver.py:167-168, 297-300);
+ * mode 2 (precision DYFOX_FP32 only): mode 0 in the float-float arithmetic
+ *         of the mixed solve's right-hand side and residuals.
  * in0, in1, out: device (n_s, n_y, Nx) complex128.  precision DYFOX_FP32
  * applies the single-precision operators of the mixed solve. */
 int dyfox_bragg_apply(const dyfox_bragg_desc *d, int mode,

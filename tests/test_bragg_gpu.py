@@ -204,6 +204,28 @@ def test_mixed_operators_match_fp64(gpu, diamond400, small, rng):
         assert 0 < rel_l2(lo, hi) < 1e-5, mode
 
 
+def test_float_float_march_matches_fp64(gpu, diamond400, small, rng):
+    """The float-float march behind the mixed solve's right-hand side and
+    true residuals agrees with the FP64 march to FP64-class accuracy
+    (<= 1e-12 relative L2 over Nz steps), far below the solve tolerance."""
+    from dyfox_gb300.bragg import apply_operator
+    torch = gpu
+    b, cfg, seg, g = small
+    s = [float(b["s_dev"]), -2e5]
+    ys = [0.0, 0.4e-6]
+    v = rng.normal(size=(2, 2, cfg.Nx)) + 1j * rng.normal(size=(2, 2, cfg.Nx))
+    w = rng.normal(size=(2, 2, cfg.Nx)) + 1j * rng.normal(size=(2, 2, cfg.Nx))
+    vt, wt = (torch.from_numpy(a).to("cuda") for a in (v, w))
+    hi = np_(apply_operator(seg, s, cfg, ys, diamond400, g, "march",
+                            in0=wt, in1=vt))
+    ff = np_(apply_operator(seg, s, cfg, ys, diamond400, g, "march_ff",
+                            in0=wt, in1=vt, precision="fp32"))
+    assert rel_l2(ff, hi) < 1e-12
+    with pytest.raises(ValueError):
+        apply_operator(seg, s, cfg, ys, diamond400, g, "march_ff",
+                       in0=wt, in1=vt)
+
+
 def test_mixed_solve_reaches_the_fp64_tolerance(gpu, diamond400, small):
     """The mixed solve stops on the double-precision true residual: every
     system converges to <= 1e-10 and the answer matches the FP64 solve and
