@@ -474,6 +474,15 @@ def _fp64_row_checks(W, outs, n_streams=16):
     return errs
 
 
+def _instance_shape(w):
+    """Sizes of one Laue instance of the batched set, for the report."""
+    from dyfox_gb300.grid import grid_arrays
+    geo = grid_arrays(w["grid"])
+    return {"Nx": geo["Nx"], "Ny": geo["Ny"], "Nz": geo["Nz"],
+            "t_um": w["grid"].t_crystal * 1e6, "dx_um": w["grid"].dx * 1e6,
+            "segments": len(w["segs"]), "angles": len(w["s"])}
+
+
 def batched_leg(args, world):
     """Batched uneven instances: 512 seeded instances (70% Laue, 30% Bragg),
     one CUDA graph per replay (per-instance set-up, one persistent Laue
@@ -632,6 +641,8 @@ def batched_leg(args, world):
         "laue_intensity_rel_l2_vs_fp64": {
             "max": max(laue_err) if laue_err else None,
             "median": float(np.median(laue_err)) if laue_err else None,
+            "worst": _instance_shape(W[li[int(np.argmax(laue_err))]])
+            if laue_err else None,
             "checked": "central row, first and last angle, every instance"},
         "bragg_rel_l2_vs_fp64": {
             "max": max(bragg_err) if bragg_err else None,
