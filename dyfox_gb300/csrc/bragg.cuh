@@ -418,7 +418,7 @@ __device__ __forceinline__ int fft_div(int i, unsigned magic) {
     return magic ? (int)__umulhi((unsigned)i, magic) : i;
 }
 
-// One radix-R pass (R = 3, 5, 7) of `count` transforms: one thread per
+// One radix-R pass (R odd, 3..13) of `count` transforms: one thread per
 // butterfly.  Inputs are twiddled once, then the R-point DFT uses the
 // conjugate pairs r, R - r: with a_r = x_r + x_{R-r}, b_r = x_r - x_{R-r},
 // y_q = x_0 + sum a_r cos(2 pi r q / R) -+ i sum b_r sin(2 pi r q / R) and
@@ -485,10 +485,15 @@ __device__ __forceinline__ void fft_odd_pass(const C *src, C *dst, int N,
 // holding the result (src or dst).  All threads call.  C is double2 or
 // float2 (the table tw has the same type).  count * (N / 2)^2 < 2^32 keeps
 // the magic division of the item index by N / R exact.
-template <typename C>
+// BIG_ODD: register butterflies also for radices 11 and 13 (the imaging
+// kernels in single precision: 4% on 544 x 1056 images; the Bragg kernels
+// keep them off, where they would raise every kernel's register count).
+// 17 and 19 stay plain sums: their butterflies cost the imaging kernels
+// more in occupancy (128 registers) than they save.
+template <typename C, bool BIG_ODD = false>
 __device__ C *fft_run(C *src, C *dst, const FftPlan &p,
-                                   const C *__restrict__ tw, bool inv,
-                                   int count = 1, int stride = 0) {
+                      const C *__restrict__ tw, bool inv, int count = 1,
+                      int stride = 0) {
     const int N = p.n, tid = threadIdx.x, nt = blockDim.x;
     if (stride == 0) stride = N;
     int Ns = 1;
@@ -543,9 +548,13 @@ __device__ C *fft_run(C *src, C *dst, const FftPlan &p,
             fft_odd_pass<5>(src, dst, N, nb, Ns, step, ns_mg, nb_mg, count, stride, tw, inv);
         } else if (R == 7) {
             fft_odd_pass<7>(src, dst, N, nb, Ns, step, ns_mg, nb_mg, count, stride, tw, inv);
+        } else if (BIG_ODD && R == 11) {
+            fft_odd_pass<11>(src, dst, N, nb, Ns, step, ns_mg, nb_mg, count, stride, tw, inv);
+        } else if (BIG_ODD && R == 13) {
+            fft_odd_pass<13>(src, dst, N, nb, Ns, step, ns_mg, nb_mg, count, stride, tw, inv);
         } else {
-            // Larger odd factors (11, 13, 17, 19, ...): one output per
-            // thread, the plain sum over the R inputs; few registers.
+            // Other odd factors (17, 19, ...; 11 and 13 without BIG_ODD):
+            // one output per thread, the plain sum over the R inputs.
             for (int it = tid; it < N * count; it += nt) {
                 const int c = count > 1 ? it / N : 0, o = it - c * N;
                 const C *sc = src + (size_t)c * stride;

@@ -74,6 +74,11 @@ __global__ void optics_twiddle_kernel(C *tw, int N) {
     tw[m] = v;
 }
 
+// Register butterflies for radices 11 and 13 in single precision only (in
+// double they would cost occupancy).
+template <typename C> constexpr bool kBigOdd = false;
+template <> constexpr bool kBigOdd<float2> = true;
+
 // Copy of the stack with every row transformed along x (forward).  One CTA
 // per (image, row).
 template <typename C>
@@ -84,7 +89,7 @@ __global__ void fft_rows_kernel(const C *__restrict__ in, C *out, int Nx,
     const size_t row = (size_t)blockIdx.x * Nx;
     for (int x = threadIdx.x; x < Nx; x += blockDim.x) a[x] = in[row + x];
     __syncthreads();
-    C *r = fft_run(a, b, plan, tw, false);
+    C *r = fft_run<C, kBigOdd<C>>(a, b, plan, tw, false);
     for (int x = threadIdx.x; x < Nx; x += blockDim.x) out[row + x] = r[x];
 }
 
@@ -110,7 +115,7 @@ __global__ void cols_pupil_kernel(C *data, int Ny, int Nx, int CB,
     }
     __syncthreads();
     // The nc columns are transformed together (one barrier per pass).
-    C *res = fft_run(a, b, plan, tw, false, nc, S);
+    C *res = fft_run<C, kBigOdd<C>>(a, b, plan, tw, false, nc, S);
     for (int t = threadIdx.x; t < Ny * CB; t += blockDim.x) {
         const int y = t / CB, c = t - y * CB;
         if (c >= nc) continue;
@@ -121,7 +126,7 @@ __global__ void cols_pupil_kernel(C *data, int Ny, int Nx, int CB,
     }
     __syncthreads();
     C *other = res == a ? b : a;
-    C *fin = fft_run(res, other, plan, tw, true, nc, S);
+    C *fin = fft_run<C, kBigOdd<C>>(res, other, plan, tw, true, nc, S);
     for (int t = threadIdx.x; t < Ny * CB; t += blockDim.x) {
         const int y = t / CB, c = t - y * CB;
         if (c < nc) base[(size_t)y * Nx + x0 + c] = fin[c * S + y];
@@ -154,7 +159,7 @@ __global__ void rows_intensity_kernel(const C *__restrict__ data, int n,
         const size_t row = ((size_t)e * Ny + y) * Nx;
         for (int x = threadIdx.x; x < Nx; x += blockDim.x) a[x] = data[row + x];
         __syncthreads();
-        const C *r = fft_run(a, b, plan, tw, true);
+        const C *r = fft_run<C, kBigOdd<C>>(a, b, plan, tw, true);
         double part = 0.0;
         for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
             // |.|^2 in the stack's precision, as the reference's abs()**2.
