@@ -24,13 +24,10 @@ __device__ double2 cmul(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-__global__ void laue_setup_kernel(const double *__restrict__ s_dev, int n_e,
-                                  int nsteps, double ds, double s0r,
-                                  double s0i, double shr, double shi,
-                                  double sbr, double sbi, Kappa *kappa,
-                                  float4 *kappa32, double2 *scale,
-                                  float *kpair) {
-    const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void laue_setup_item(
+    long idx, const double *__restrict__ s_dev, int n_e, int nsteps,
+    double ds, double s0r, double s0i, double shr, double shi, double sbr,
+    double sbi, Kappa *kappa, float4 *kappa32, double2 *scale, float *kpair) {
     if (idx >= (long)n_e * nsteps) return;
     const int ie = (int)(idx / nsteps), k = (int)(idx - (long)ie * nsteps);
     const double alpha = -2.0 * kPi * s_dev[ie];
@@ -87,6 +84,17 @@ __global__ void laue_setup_kernel(const double *__restrict__ s_dev, int n_e,
         }
         scale[ie] = acc;
     }
+}
+
+__global__ void laue_setup_kernel(const double *__restrict__ s_dev, int n_e,
+                                  int nsteps, double ds, double s0r,
+                                  double s0i, double shr, double shi,
+                                  double sbr, double sbi, Kappa *kappa,
+                                  float4 *kappa32, double2 *scale,
+                                  float *kpair) {
+    laue_setup_item(blockIdx.x * (long)blockDim.x + threadIdx.x, s_dev, n_e,
+                    nsteps, ds, s0r, s0i, shr, shi, sbr, sbi, kappa, kappa32,
+                    scale, kpair);
 }
 
 // e^{iH(kk, x)} from a cheap source, for the general march.
@@ -199,18 +207,61 @@ __global__ void laue_general_kernel(const MarchArgs a, R shift_px) {
 // Rows with |y| >= fov_hy are written as zero (kernels.py:70-75).  Rows
 // start on 8-byte boundaries (complex64 or complex128 elements), so the
 // stores are 8 bytes wide; blocks stride over the (angle, row) pairs.
-__global__ void zero_rows_kernel(char *out, int n_e, int Ny, size_t row_bytes,
-                                 int row0, int n_rows) {
+// Rows outside the beam of every angle set to zero; block b of nb.
+__device__ __forceinline__ void zero_rows_blocks(char *out, int n_e, int Ny,
+                                                 size_t row_bytes, int row0,
+                                                 int n_rows, int b, int nb) {
     const int n_inactive = Ny - n_rows;
     const long pairs = (long)n_e * n_inactive;
     const size_t words = row_bytes / 8;
-    for (long r = blockIdx.x; r < pairs; r += gridDim.x) {
+    for (long r = b; r < pairs; r += nb) {
         const int ie = (int)(r / n_inactive);
         const int j = (int)(r - (long)ie * n_inactive);
         const int iy = j < row0 ? j : j + n_rows;
         uint2 *p = reinterpret_cast<uint2 *>(out + ((size_t)ie * Ny + iy) * row_bytes);
         for (size_t i = threadIdx.x; i < words; i += blockDim.x)
             p[i] = make_uint2(0, 0);
+    }
+}
+
+__global__ void zero_rows_kernel(char *out, int n_e, int Ny, size_t row_bytes,
+                                 int row0, int n_rows) {
+    zero_rows_blocks(out, n_e, Ny, row_bytes, row0, n_rows, blockIdx.x,
+                     gridDim.x);
+}
+
+// The set-up of one solve in one launch: blocks [0, nz) zero the rows
+// outside the beam, the next ns blocks compute the kappa tables, the last
+// np blocks the segment pivots of a fused single-precision march.  The three
+// are independent; as separate launches they ran one after another
+// (about 60 us on the README workload, most of it double-precision latency).
+struct PrologueArgs {
+    // zero rows
+    char *out; int n_e, Ny; size_t row_bytes; int row0, n_rows;
+    // kappa tables
+    const double *s_dev; int nsteps;
+    double ds, s0r, s0i, shr, shi, sbr, sbi;
+    Kappa *kappa; float4 *kappa32; double2 *scale; float *kpair;
+    // pivots
+    const double *segs; int n_seg, Nx; double dx, dz; float4 *piv;
+    int nz, ns, np;
+};
+
+__global__ void laue_prologue_kernel(const PrologueArgs a) {
+    const int b = blockIdx.x;
+    if (b < a.nz) {
+        zero_rows_blocks(a.out, a.n_e, a.Ny, a.row_bytes, a.row0, a.n_rows, b,
+                         a.nz);
+    } else if (b < a.nz + a.ns) {
+        laue_setup_item((long)(b - a.nz) * blockDim.x + threadIdx.x, a.s_dev,
+                        a.n_e, a.nsteps, a.ds, a.s0r, a.s0i, a.shr, a.shi,
+                        a.sbr, a.sbi, a.kappa, a.kappa32, a.scale, a.kpair);
+    } else {
+        const long total = (long)a.n_rows * a.nsteps * a.n_seg;
+        for (long i = (long)(b - a.nz - a.ns) * blockDim.x + threadIdx.x;
+             i < total; i += (long)a.np * blockDim.x)
+            pivot_item(i, a.segs, a.n_seg, a.Nx, a.Ny, a.dx, a.dz, a.row0,
+                       a.nsteps, a.piv);
     }
 }
 
@@ -574,26 +625,41 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     a.kpair = single ? (const float4 *)(ws + p.off_kpair) : nullptr;
 
     cudaError_t e;
-    // Rows outside the beam are zero.
-    if ((e = launch_zero_rows(d, out, elem, p.row0, p.n_rows, stream)))
-        return cuda_status(e, "zero_rows");
-    if (p.n_rows == 0) return DYFOX_OK;
-    if ((e = launch_laue_setup(d, s_dev, (Kappa *)(ws + p.off_kappa),
-                               (float4 *)(ws + p.off_k32),
-                               (double2 *)(ws + p.off_scale),
-                               single ? (float4 *)(ws + p.off_kpair) : nullptr,
-                               stream)))
-        return cuda_status(e, "laue_setup");
-    if (p.hsrc == HS_SEG && single) {
-        const long n = (long)p.n_rows * nsteps * d->n_seg;
-        long blocks = (n + 255) / 256;
-        if (blocks > 152L * 32) blocks = 152L * 32;
-        pivot_kernel<<<(int)blocks, 256, 0, stream>>>(
-            seg_table, d->n_seg, d->Nx, d->Ny, d->dx, d->dz, p.row0, p.n_rows,
-            nsteps, (float4 *)(ws + p.off_piv));
-        count_launch(1);
-        if ((e = cudaGetLastError())) return cuda_status(e, "pivot");
+    // Rows outside the beam are zero; kappa tables; pivots (one launch).
+    {
+        PrologueArgs pa;
+        memset(&pa, 0, sizeof pa);
+        pa.out = (char *)out; pa.n_e = d->n_e; pa.Ny = d->Ny;
+        pa.row_bytes = (size_t)d->Nx * elem; pa.row0 = p.row0;
+        pa.n_rows = p.n_rows;
+        pa.s_dev = s_dev; pa.nsteps = nsteps;
+        pa.ds = d->ds; pa.s0r = d->sig0[0]; pa.s0i = d->sig0[1];
+        pa.shr = d->sig_h[0]; pa.shi = d->sig_h[1];
+        pa.sbr = d->sig_hbar[0]; pa.sbi = d->sig_hbar[1];
+        pa.kappa = (Kappa *)(ws + p.off_kappa);
+        pa.kappa32 = (float4 *)(ws + p.off_k32);
+        pa.scale = (double2 *)(ws + p.off_scale);
+        pa.kpair = single ? (float *)(ws + p.off_kpair) : nullptr;
+        pa.segs = seg_table; pa.n_seg = d->n_seg; pa.Nx = d->Nx;
+        pa.dx = d->dx; pa.dz = d->dz; pa.piv = (float4 *)(ws + p.off_piv);
+        const long zpairs = p.n_rows < d->Ny ? (long)d->n_e * (d->Ny - p.n_rows)
+                                              : 0;
+        pa.nz = (int)(zpairs < 152L * 16 ? zpairs : 152L * 16);
+        pa.ns = p.n_rows ? (int)(((long)d->n_e * nsteps + 255) / 256) : 0;
+        long pv = 0;
+        if (p.n_rows && p.hsrc == HS_SEG && single) {
+            pv = ((long)p.n_rows * nsteps * d->n_seg + 255) / 256;
+            if (pv > 152L * 32) pv = 152L * 32;
+        }
+        pa.np = (int)pv;
+        const int blocks = pa.nz + pa.ns + pa.np;
+        if (blocks > 0) {
+            laue_prologue_kernel<<<blocks, 256, 0, stream>>>(pa);
+            count_launch(1);
+            if ((e = cudaGetLastError())) return cuda_status(e, "prologue");
+        }
     }
+    if (p.n_rows == 0) return DYFOX_OK;
     if (p.stage) {
         e = launch_cs_stage(single, (d->flags & DYFOX_FLAG_H_FP64) != 0,
                             seg_table, d->n_seg, d->Nx, d->Ny,

@@ -110,15 +110,8 @@ __global__ void pivot_kernel(const double *__restrict__ segs, int n_seg,
                              int n_rows, int nsteps, float4 *out) {
     const long total = (long)n_rows * nsteps * n_seg;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total;
-         i += (long)gridDim.x * blockDim.x) {
-        const int s = (int)(i % n_seg);
-        const long t = i / n_seg;
-        const int k = (int)(t % nsteps);
-        const int r = (int)(t / nsteps);
-        const double y_pix = (row0 + r - Ny / 2) * dx;
-        out[i] = seg_pivot(segs + (size_t)s * DYFOX_SEG_STRIDE, y_pix, k * dz,
-                           Nx, dx);
-    }
+         i += (long)gridDim.x * blockDim.x)
+        pivot_item(i, segs, n_seg, Nx, Ny, dx, dz, row0, nsteps, out);
 }
 
 cudaError_t launch_cs_stage(bool single, bool sum64, const double *segs,
