@@ -74,8 +74,10 @@ __global__ void optics_twiddle_kernel(C *tw, int N) {
     tw[m] = v;
 }
 
-// Register butterflies for radices 11 and 13 in single precision only (in
-// double they would cost occupancy).
+// Register butterflies for radices 11 and 13 in the row passes in single
+// precision only (in double, and in the column pass that holds a block of
+// columns in shared memory, the extra registers cost more occupancy than
+// the butterflies save).
 template <typename C> constexpr bool kBigOdd = false;
 template <> constexpr bool kBigOdd<float2> = true;
 
@@ -115,7 +117,7 @@ __global__ void cols_pupil_kernel(C *data, int Ny, int Nx, int CB,
     }
     __syncthreads();
     // The nc columns are transformed together (one barrier per pass).
-    C *res = fft_run<C, kBigOdd<C>>(a, b, plan, tw, false, nc, S);
+    C *res = fft_run<C, false>(a, b, plan, tw, false, nc, S);
     for (int t = threadIdx.x; t < Ny * CB; t += blockDim.x) {
         const int y = t / CB, c = t - y * CB;
         if (c >= nc) continue;
@@ -126,7 +128,7 @@ __global__ void cols_pupil_kernel(C *data, int Ny, int Nx, int CB,
     }
     __syncthreads();
     C *other = res == a ? b : a;
-    C *fin = fft_run<C, kBigOdd<C>>(res, other, plan, tw, true, nc, S);
+    C *fin = fft_run<C, false>(res, other, plan, tw, true, nc, S);
     for (int t = threadIdx.x; t < Ny * CB; t += blockDim.x) {
         const int y = t / CB, c = t - y * CB;
         if (c < nc) base[(size_t)y * Nx + x0 + c] = fin[c * S + y];
