@@ -359,6 +359,17 @@ bragg_gmres_kernel(const BraggArgs a) {
     solve_system<CPL, MIXED>(a, blockIdx.x, smem);
 }
 
+// The mixed 4-column, 128-thread kernel (config 1's shape) with bounds that
+// keep 5 CTAs per SM (96 registers instead of 122: 4% on config 1).  Bounds
+// on every instantiation would let the others take 186-234 registers.
+// (a template so that only the unit that launches it compiles it)
+template <int NT>
+__global__ void __launch_bounds__(NT, 5)
+bragg_gmres_mixed4_kernel(const BraggArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    solve_system<4, true>(a, blockIdx.x, smem);
+}
+
 // After a mixed launch: one CTA per system, returning at once unless the
 // system was marked.
 template <int CPL, int NT>
@@ -441,6 +452,9 @@ static cudaError_t resident(K *k, int threads, size_t smem) {
 // CPL 1, 2 only occur with 128 threads, 8 and 16 only with 256.
 template <int CPL, bool MIXED>
 static void (*gmres_kernel_for(int threads))(const BraggArgs) {
+    if constexpr (CPL == 4 && MIXED) {
+        if (threads == 128) return bragg_gmres_mixed4_kernel<128>;
+    }
     if constexpr (CPL <= 2) {
         return bragg_gmres_kernel<CPL, MIXED, 128>;
     } else if constexpr (CPL >= 8) {
