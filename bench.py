@@ -366,7 +366,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "voxel-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (two-sum compensated)",
+        "vs_baseline": None, "dtype": "f32 (compensated)",
         "data": "synthetic (seeded geometry of the benchmark configuration)",
         "config": {"workload": WORKLOAD, "angles": n_e,
                    "active_rows": int(len(rows)), "Nx": geo["Nx"],

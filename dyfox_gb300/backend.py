@@ -3,8 +3,10 @@
 Mirrors DYFOX ``backend.py:49-99``: ``FP64`` and ``FP32`` objects carry their
 NumPy/torch dtypes and are passed to the solvers as ``precision=``.  FP64 is
 the parity mode (double everywhere).  FP32 here is the compensated mode: a
-single-precision march with two-sum compensated amplitude updates, with the
-displacement phase summed over segments and reduced mod 2 pi in double.
+single-precision march with compensated (Fast2Sum) amplitude updates, the
+displacement phase summed over segments and reduced mod 2 pi in
+float-float (or in double, ``h_sum="fp64"``); in the Bragg solve,
+single-precision Krylov products with float-float residuals.
 Results come back as torch CUDA tensors; ``to_numpy`` copies any of them to
 the host.
 """
