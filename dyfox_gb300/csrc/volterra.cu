@@ -105,15 +105,6 @@ __global__ void cs_stage_kernel(const double *__restrict__ segs, int n_seg,
     }
 }
 
-__global__ void pivot_kernel(const double *__restrict__ segs, int n_seg,
-                             int Nx, int Ny, double dx, double dz, int row0,
-                             int n_rows, int nsteps, float4 *out) {
-    const long total = (long)n_rows * nsteps * n_seg;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total;
-         i += (long)gridDim.x * blockDim.x)
-        pivot_item(i, segs, n_seg, Nx, Ny, dx, dz, row0, nsteps, out);
-}
-
 cudaError_t launch_cs_stage(bool single, bool sum64, const double *segs,
                             int n_seg, int Nx, int Ny, int Nz, double dx,
                             double dz,
