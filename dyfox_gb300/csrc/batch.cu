@@ -14,9 +14,11 @@
 // staging of the slab rows).  H is evaluated once per voxel and never
 // stored beyond one row per resident CTA.
 //
-// Bragg: after each instance's couplings / symbol set-up, one launch of one
-// CTA per (instance, deviation parameter, plane) system, the systems of the
-// largest planes first; one launch per precision present.
+// Bragg: after each instance's couplings / symbol set-up, one CTA per
+// (instance, deviation parameter, plane) system, the systems of the largest
+// planes first; one launch per launch shape present (precision, threads and
+// columns per thread as a single solve of the instance would take them, so
+// that narrow planes do not run at the shape of the widest).
 #include <math.h>
 #include <string.h>
 
@@ -143,7 +145,18 @@ struct LaueB {
 struct BraggB {
     int item;
     bool mixed;
+    int group;                           // index into BatchLayout::bgroups
     size_t off_ws, bytes, off_y;
+};
+
+// Bragg systems that share one launch shape: precision, threads per CTA and
+// columns per thread, as a single solve of each instance would choose them.
+struct BraggGroup {
+    bool mixed;
+    int threads, cpl;
+    size_t smem = 0;
+    int n_sys = 0;
+    size_t off_sys = 0;
 };
 
 struct BatchLayout {
@@ -152,11 +165,9 @@ struct BatchLayout {
     int cpl = 5, warps = 8, ctas_per_sm = 0, grid = 0;
     size_t smem_laue = 0, slab_elems = 0;
     long n_items = 0;
-    int n_sys[2] = {0, 0};                // FP64, mixed
-    int b_threads = 0, b_cpl = 1;
-    size_t b_smem = 0;
+    std::vector<BraggGroup> bgroups;
     size_t off_linst = 0, off_items = 0, off_ticket = 0, off_slabs = 0,
-           off_binst = 0, off_sys[2] = {0, 0}, ws = 0;
+           off_binst = 0, ws = 0;
 };
 
 static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -259,9 +270,23 @@ static int batch_plan(const dyfox_batch_item *items, int n,
             b.off_ws = off; off = al256(off + bytes);
             b.bytes = bytes;
             b.off_y = off; off = al256(off + d->n_y * sizeof(double));
-            L->n_sys[b.mixed ? 1 : 0] += d->n_y * d->n_s;
-            L->b_threads = std::max(L->b_threads, threads);
-            L->b_smem = std::max(L->b_smem, bragg_instance_smem(d));
+            b.group = -1;
+            for (size_t g = 0; g < L->bgroups.size(); ++g) {
+                const BraggGroup &G = L->bgroups[g];
+                if (G.mixed == b.mixed && G.threads == threads && G.cpl == bc)
+                    b.group = (int)g;
+            }
+            if (b.group < 0) {
+                BraggGroup G;
+                G.mixed = b.mixed;
+                G.threads = threads;
+                G.cpl = bc;
+                L->bgroups.push_back(G);
+                b.group = (int)L->bgroups.size() - 1;
+            }
+            BraggGroup &G = L->bgroups[b.group];
+            G.n_sys += d->n_y * d->n_s;
+            G.smem = std::max(G.smem, bragg_instance_smem(d));
             L->bragg.push_back(b);
         } else {
             set_error("item %d: unknown kind %d", i, it.kind);
@@ -271,18 +296,6 @@ static int batch_plan(const dyfox_batch_item *items, int n,
     if (L->n_items > (1L << 30)) {
         set_error("%ld Laue items, above 2^30", L->n_items);
         return DYFOX_ENOSYS;
-    }
-    // Bragg: one thread count for all; columns per thread cover max Nx.
-    if (!L->bragg.empty()) {
-        int max_nx = 0;
-        for (const BraggB &b : L->bragg)
-            max_nx = std::max(max_nx, items[b.item].bragg.Nx);
-        L->b_cpl = pow2_at_least(div_up(max_nx, L->b_threads));
-        if (L->b_cpl > 16) {
-            set_error("Bragg Nx=%d too large for %d threads", max_nx,
-                      L->b_threads);
-            return DYFOX_ENOSYS;
-        }
     }
     // Laue persistent grid.
     if (L->n_items > 0) {
@@ -320,9 +333,9 @@ static int batch_plan(const dyfox_batch_item *items, int n,
     L->off_slabs = off;
     off = al256(off + (size_t)L->grid * L->slab_elems * sizeof(float2));
     L->off_binst = off; off = al256(off + L->bragg.size() * sizeof(BraggArgs));
-    for (int p = 0; p < 2; ++p) {
-        L->off_sys[p] = off;
-        off = al256(off + (size_t)L->n_sys[p] * sizeof(int2));
+    for (BraggGroup &G : L->bgroups) {
+        G.off_sys = off;
+        off = al256(off + (size_t)G.n_sys * sizeof(int2));
     }
     L->ws = off;
     return DYFOX_OK;
@@ -395,12 +408,12 @@ static int record_batch(const dyfox_batch_item *items, const BatchLayout &L,
         count_launch(1);
         if ((e = cudaGetLastError())) return cuda_status(e, "laue_batch");
     }
-    for (int p = 0; p < 2; ++p) {
-        if (!L.n_sys[p]) continue;
+    // One launch per launch shape (largest systems first within each).
+    for (const BraggGroup &G : L.bgroups) {
+        if (!G.n_sys) continue;
         if ((e = launch_bragg_batch((const BraggArgs *)(ws + L.off_binst),
-                                    (const int2 *)(ws + L.off_sys[p]),
-                                    L.n_sys[p], L.b_threads, L.b_cpl, p == 1,
-                                    L.b_smem, s)))
+                                    (const int2 *)(ws + G.off_sys), G.n_sys,
+                                    G.threads, G.cpl, G.mixed, G.smem, s)))
             return cuda_status(e, "bragg_batch");
     }
     return DYFOX_OK;
@@ -471,15 +484,15 @@ extern "C" int dyfox_batch_create(const dyfox_batch_item *items, int n,
                      });
     std::vector<int2> qitems(q.size());
     for (size_t i = 0; i < q.size(); ++i) qitems[i] = q[i].second;
-    std::vector<std::pair<double, int2>> sys[2];
+    std::vector<std::vector<std::pair<double, int2>>> sys(L.bgroups.size());
     for (size_t j = 0; j < L.bragg.size(); ++j) {
         const dyfox_bragg_desc *d = &items[L.bragg[j].item].bragg;
         const double cost = (double)d->Nz * d->Nx;
-        const int p = L.bragg[j].mixed ? 1 : 0;
+        const int p = L.bragg[j].group;
         for (int k = 0; k < d->n_y * d->n_s; ++k)
             sys[p].push_back({cost, make_int2((int)j, k)});
     }
-    for (int p = 0; p < 2; ++p)
+    for (size_t p = 0; p < sys.size(); ++p)
         std::stable_sort(sys[p].begin(), sys[p].end(),
                          [](const std::pair<double, int2> &x,
                             const std::pair<double, int2> &y) {
@@ -497,11 +510,11 @@ extern "C" int dyfox_batch_create(const dyfox_batch_item *items, int n,
                              qitems.size() * sizeof(int2),
                              cudaMemcpyHostToDevice, stream)))
         return cuda_status(e, "batch upload");
-    for (int p = 0; p < 2; ++p) {
+    for (size_t p = 0; p < sys.size(); ++p) {
         std::vector<int2> v(sys[p].size());
         for (size_t i = 0; i < v.size(); ++i) v[i] = sys[p][i].second;
         if (!v.empty() &&
-            (e = cudaMemcpyAsync(ws + L.off_sys[p], v.data(),
+            (e = cudaMemcpyAsync(ws + L.bgroups[p].off_sys, v.data(),
                                  v.size() * sizeof(int2),
                                  cudaMemcpyHostToDevice, stream)))
             return cuda_status(e, "batch upload");
@@ -517,10 +530,9 @@ extern "C" int dyfox_batch_create(const dyfox_batch_item *items, int n,
     }
     if ((e = cudaStreamSynchronize(stream)))
         return cuda_status(e, "batch upload");
-    for (int p = 0; p < 2; ++p)
-        if (L.n_sys[p] &&
-            (e = set_bragg_batch_smem(L.b_cpl, p == 1, L.b_smem,
-                                      L.b_threads)))
+    for (const BraggGroup &G : L.bgroups)
+        if (G.n_sys &&
+            (e = set_bragg_batch_smem(G.cpl, G.mixed, G.smem, G.threads)))
             return cuda_status(e, "bragg_batch attributes");
 
     // Capture the graph on a private stream.

@@ -235,9 +235,10 @@ int dyfox_bragg_symbol(const dyfox_bragg_desc *d, const double *s_dev,
  *     launch over a cost-sorted queue of (instance, row) items: the CTA that
  *     takes an item stages e^{iH} of that row once into its own slab and
  *     marches every angle group of the instance through it;
- *   * every Bragg instance's couplings / symbol set-up, then ONE launch of
- *     one CTA per (instance, deviation parameter, plane) system, longest
- *     first (one launch per precision present).
+ *   * every Bragg instance's couplings / symbol set-up, then one CTA per
+ *     (instance, deviation parameter, plane) system, longest first: one
+ *     launch per launch shape present (precision, threads, columns per
+ *     thread, as a single solve of the instance would choose them).
  * Laue items: precision DYFOX_FP32 (compensated march), h_source
  * DYFOX_H_SEGMENTS or DYFOX_H_NONE, shift_px == 1, Nx even and at most
  * 32 * cols_per_lane * warps; flags DYFOX_FLAG_H_FP64 sums the segment
