@@ -233,10 +233,11 @@ static int image_plan(int n, int Ny, int Nx, int precision, ImagePlan *p) {
                   Ny, Nx);
         return DYFOX_EINVAL;
     }
-    // Columns per block of the column pass: 8 where they fit in half the
-    // shared memory and keep the batched transform's index division exact
-    // (CB (Ny / 2)^2 < 2^32).
-    p->CB = 8;
+    // Columns per block of the column pass: 4 (against 8: 3% faster on
+    // 544 x 1056 images, twice the resident blocks per SM), fewer where they
+    // would not fit in half the shared memory or would break the exactness
+    // of the batched transform's index division (CB (Ny / 2)^2 < 2^32).
+    p->CB = 4;
     while (p->CB > 1 &&
            (2 * (size_t)p->CB * (Ny + 1) * cs > (size_t)optin / 2 ||
             (unsigned long long)p->CB * (Ny / 2) * (Ny / 2) >= (1ull << 32)))
