@@ -241,6 +241,17 @@ def solve_batch(instances, **kw):
 CANDIDATES = ((5, 8), (7, 8), (9, 8), (11, 8), (5, 16), (7, 16), (5, 4))
 
 
+def pick_shape(times, tie=0.01):
+    """The (cols_per_lane, warps) of ``times`` {shape: ms} to use: shapes
+    within ``tie`` of the fastest are a tie, won by the fewest warps a CTA
+    (smaller CTAs balance the persistent queue better on the whole set:
+    3.22 against 3.41 s for 4 against 8 warps on the 512-instance set,
+    0.03% apart on its tuning sample), then by time."""
+    fastest = min(times.values())
+    return min((k for k, t in times.items() if t <= (1.0 + tie) * fastest),
+               key=lambda k: (k[1], times[k]))
+
+
 def autotune(instances, candidates=CANDIDATES, sample=48, repeats=2,
              h_sum="ff", seed=0, verbose=False):
     """Launch shape of the batched Laue march: times a batch of ``sample``
@@ -275,12 +286,6 @@ def autotune(instances, candidates=CANDIDATES, sample=48, repeats=2,
         del b
     if not times:
         raise NotImplementedError("no launch shape holds these instances")
-    # Shapes within 1% of the fastest on the sample are a tie; the one with
-    # the fewest warps a CTA wins it (smaller CTAs balance the persistent
-    # queue better on the whole set: 3.22 against 3.41 s for 4 against 8
-    # warps on the 512-instance set, 0.03% apart on its sample).
-    fastest = min(times.values())
-    best = min((k for k, t in times.items() if t <= 1.01 * fastest),
-               key=lambda k: (k[1], times[k]))
+    best = pick_shape(times)
     return {"cols_per_lane": best[0], "warps": best[1],
             "ms": {f"{c}x{w}": t for (c, w), t in times.items()}}

@@ -27,3 +27,13 @@ def test_batched_uneven_mix_and_ranges():
             assert 1 <= len(w["ys"]) <= 8
             assert 5e-6 - c.dz <= c.t_crystal <= 20e-6 + c.dz
             assert c.Nx == 2 * (round(c.half_x / c.dx) + 2 * c.Nz + 16)
+
+
+def test_batch_shape_pick_breaks_near_ties_toward_fewer_warps():
+    from dyfox_gb300.batch import pick_shape
+    t = {(5, 8): 433.8, (5, 4): 433.9, (7, 8): 510.2, (5, 16): 532.3}
+    assert pick_shape(t) == (5, 4)
+    # outside the 1% window the faster shape wins
+    assert pick_shape({(5, 8): 400.0, (5, 4): 420.0}) == (5, 8)
+    # among equal warps, the faster
+    assert pick_shape({(5, 4): 101.0, (7, 4): 100.0}) == (7, 4)
