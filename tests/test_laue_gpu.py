@@ -423,3 +423,26 @@ def test_autotuner_caches_a_shape_that_changes_nothing(gpu, diamond400,
     after = np_(solve_dislocation(seg, s, small_grid, diamond400,
                                   precision="fp32"))
     assert before.tobytes() == after.tobytes()
+
+
+def test_wave_cache_solves_once_and_reloads(gpu, diamond400, small_grid,
+                                            tmp_path):
+    """A miss solves and stores complex64 under the key's file name; a hit
+    reads it back; other inputs get another file."""
+    import os
+    from dyfox_gb300.cache import WaveCache
+    from dyfox_gb300.laue import solve_dislocation
+    torch = gpu
+    seg = geometry_n(diamond400, small_grid)
+    s = [0.0, 1e5]
+    cache = WaveCache(str(tmp_path))
+    a = cache.solve(seg, s, small_grid, diamond400)
+    path = cache.path(seg, s, small_grid, diamond400)
+    assert os.path.exists(path)
+    ref = np_(solve_dislocation(seg, s, small_grid, diamond400))
+    assert np.array_equal(np_(a), ref)
+    b = cache.solve(seg, s, small_grid, diamond400)
+    assert b.dtype == torch.complex64 and b.is_cuda
+    assert np.array_equal(np_(b), ref.astype(np.complex64))
+    cache.solve(seg, [0.0], small_grid, diamond400)
+    assert len(os.listdir(tmp_path)) == 2
