@@ -339,6 +339,8 @@ def run_ours(args):
     mean_ms = 1e3 * tot / args.steps
     plain_ms = statistics.mean(ms_plain)
 
+    h_variants = None if args.once else readme_h_variants(seg, s, grid, x)
+
     # e2e: public API, host inputs, device-to-host read of the exit waves
     host = torch.empty((n_e, geo["Ny"], geo["Nx"]), dtype=torch.complex64,
                        pin_memory=True)
@@ -406,6 +408,7 @@ def run_ours(args):
                                       "2048 CTAs)"},
         "gpu_launches": int(launches),
         "wall_s": wall,
+        "h_variants": h_variants,
     }
     clk_sum = clk.summary()
     line["clocks"] = clk_sum
@@ -840,6 +843,60 @@ def scan_leg(args, world):
             "intensity_rel_l2_vs_fp64_8_angles": err,
             "fp64_8_angles_s": fp64_s, "gpu_launches": int(launches),
             "launch_shape": shape}
+
+
+def readme_h_variants(seg, s, grid, x, reps=5):
+    """The README step (FP32 compensated march) with the Volterra phase
+    fused into the march, against e^{iH} staged once in the workspace and
+    against the reference's layout: the whole H grid (Ny, Nz, Nx) built in
+    HBM first (compute_H_grid, float32 or float64) and read by the march.
+    All through solve_dislocation, L2 flushed before each call; ms medians
+    and the intensity error of each against the plain FP64 solve."""
+    import torch
+    from dyfox_gb300.dislocations import compute_H_grid
+    from dyfox_gb300.laue import solve_dislocation
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ref = solve_dislocation(seg, s, grid, x, precision="fp64")
+    I64 = ref.abs() ** 2
+
+    def timed(fn, check=True):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            out = fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        if not check:
+            return statistics.median(ts), None
+        I = out.abs().double() ** 2
+        err = float(torch.linalg.vector_norm(I - I64) /
+                    torch.linalg.vector_norm(I64))
+        return statistics.median(ts), err
+
+    res = {}
+    for name, mode in (("fused", "fused"), ("staged_cs", "staged")):
+        ms, err = timed(lambda: solve_dislocation(seg, s, grid, x,
+                                                  precision="fp32",
+                                                  h_mode=mode))
+        res[name] = {"ms": ms, "intensity_rel_l2": err}
+    for name, hp in (("h_grid_f32", "fp32"), ("h_grid_f64", "fp64")):
+        H = compute_H_grid(seg, grid, x, precision=hp)
+        h_ms, _ = timed(lambda: compute_H_grid(seg, grid, x, precision=hp),
+                        check=False)
+        m_ms, err = timed(lambda: solve_dislocation(seg, s, grid, x,
+                                                    H_gpu=H,
+                                                    precision="fp32"))
+        res[name] = {"ms": h_ms + m_ms, "h_grid_ms": h_ms, "march_ms": m_ms,
+                     "h_grid_bytes": int(H.numel() * H.element_size()),
+                     "intensity_rel_l2": err}
+        del H
+    return res
 
 
 def hbm_peak():
