@@ -413,7 +413,7 @@ def run_ours(args):
     clk_sum = clk.summary()
     line["clocks"] = clk_sum
     if not args.no_bragg:
-        line["bragg"] = bragg_leg(args, rank, world)
+        line["bragg"] = bragg_leg(args, rank, world, peaks)
     if not args.no_scan:
         line["laue_scan"] = scan_leg(args, world)
     if not args.no_com_maps:
@@ -1006,7 +1006,25 @@ def com_maps_leg(args, world):
             "max_com_deviation_urad_vs_fp64_16_angles": dev}
 
 
-def bragg_leg(args, rank, world):
+def bragg_flops(inf, Nx, Nz, restart):
+    """Algorithmic flops of a scan's solves from the per-system inner
+    iteration counts (info column 1): per inner iteration the march
+    (28 (Nz - 1) Nx), the preconditioner (two Nx-point FFTs, 5 N log2 N
+    each, and the 1/T22s product, 6 Nx) and modified Gram-Schmidt against
+    the j + 1 basis vectors of the cycle (16 (j + 1) Nx); per system two
+    more marches (right-hand side and at least one true residual).  Returns
+    (Krylov-product flops, Gram-Schmidt flops)."""
+    march = 28.0 * (Nz - 1) * Nx
+    prec = 2 * 5.0 * Nx * np.log2(Nx) + 6.0 * Nx
+    prod = mgs = 0.0
+    for it in inf[:, 1].astype(int):
+        prod += it * (march + prec) + 2 * march
+        j = np.arange(it) % restart
+        mgs += float(np.sum(16.0 * (j + 1) * Nx))
+    return prod, mgs
+
+
+def bragg_leg(args, rank, world, peaks=None):
     """Bragg solves/s of config 1: all 21 deviation parameters x 64 planes
     in one batched launch (one solve = one deviation parameter over all
     planes, to true relative residual <= 1e-10).  The chosen form is the
@@ -1062,6 +1080,25 @@ def bragg_leg(args, rank, world):
                           "ms_per_scan": ms64,
                           "max_true_residual": float(inf64[:, 0].max()),
                           "max_inner_iterations": int(inf64[:, 1].max())}}
+    if peaks:
+        # Pipe roofline of both forms (TFLOP/s of the algorithmic count).
+        p32, g32 = bragg_flops(inf, cfg.Nx, cfg.Nz, 40)
+        p64, g64 = bragg_flops(inf64, cfg.Nx, cfg.Nz, 40)
+        t32, t64 = ms * 1e-3 * 1e12, ms64 * 1e-3 * 1e12
+        res["roofline"] = {
+            "bound": "latency (FP32 Krylov products, FP64 Gram-Schmidt)",
+            "algorithmic_gflop_per_scan": (p32 + g32) * 1e-9,
+            "fp32_part_tflops": world * p32 / t32,
+            "fp32_part_frac": world * p32 / t32 / peaks["fp32"],
+            "fp64_part_tflops": world * g32 / t32,
+            "fp64_part_frac": world * g32 / t32 / peaks["fp64"],
+            "unit": "TFLOP/s", "peak_source": "measured FMA throughput "
+            "(dyfox_pipe_peak, this run)"}
+        res["plain_fp64"]["roofline"] = {
+            "bound": "fp64", "achieved": world * (p64 + g64) / t64,
+            "peak": peaks["fp64"], "unit": "TFLOP/s",
+            "frac": world * (p64 + g64) / t64 / peaks["fp64"],
+            "algorithmic_gflop_per_scan": (p64 + g64) * 1e-9}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import bragg_oracle as BO
         t0 = time.perf_counter()
