@@ -415,7 +415,7 @@ def run_ours(args):
     if not args.no_bragg:
         line["bragg"] = bragg_leg(args, rank, world, peaks)
     if not args.no_scan:
-        line["laue_scan"] = scan_leg(args, world)
+        line["laue_scan"] = scan_leg(args, world, peaks)
     if not args.no_com_maps:
         line["com_maps"] = com_maps_leg(args, world)
     if not args.no_batched:
@@ -783,7 +783,7 @@ def learned_leg(args, world):
     }
 
 
-def scan_leg(args, world):
+def scan_leg(args, world, peaks=None):
     """The 256-angle rocking scan (t = 273 um, 544 x 1056, Nz 490, 64 random
     <110> segments): chosen FP32 form, e^{iH} staged once (float-float
     segment sum) and read by every angle group.  Accuracy is checked
@@ -842,7 +842,18 @@ def scan_leg(args, world):
                     "(float-float segment sum), all angles in one call",
             "intensity_rel_l2_vs_fp64_8_angles": err,
             "fp64_8_angles_s": fp64_s, "gpu_launches": int(launches),
-            "launch_shape": shape}
+            "launch_shape": shape,
+            "roofline": None if not peaks else {
+                "bound": "fp32",
+                # 40 flops a voxel-step (march) and 40 a segment-voxel (the
+                # staged phase, atan2 and log not counted)
+                "achieved": world * 40.0 * (units + len(rows) * geo["Nx"] *
+                                            (geo["Nz"] - 1) * len(segs))
+                / (ms * 1e-3) / 1e12,
+                "peak": peaks["fp32"], "unit": "TFLOP/s",
+                "frac": world * 40.0 * (units + len(rows) * geo["Nx"] *
+                                        (geo["Nz"] - 1) * len(segs))
+                / (ms * 1e-3) / 1e12 / peaks["fp32"]}}
 
 
 def readme_h_variants(seg, s, grid, x, reps=5):
