@@ -1,4 +1,4 @@
-// Single-precision compensated (two-sum) instantiations of the register-resident Laue march.
+// Single-precision compensated (Fast2Sum) instantiations of the register-resident Laue march.
 #include "laue_march.cuh"
 
 namespace dyfox {
