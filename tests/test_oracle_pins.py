@@ -219,8 +219,18 @@ def test_single_precision_atan2_polynomial():
         np.float32)
     ax, ay = np.abs(x), np.abs(y)
     t = np.minimum(ax, ay) / np.maximum(ax, ay)
-    r = fa.eval_f32(c, t).astype(np.float64)
-    r = np.where(ay > ax, np.pi / 2 - r, r)
-    r = np.where(x < 0, np.pi - r, r)
-    r = np.copysign(r, y)
-    assert np.abs(r - np.arctan2(y.astype(float), x.astype(float))).max() < 3e-7
+    r = fa.eval_f32(c, t)
+    # The octant folds in float32 with pi / 2 and pi as hi + lo float pairs
+    # (the kernel's kPio2Hi/Lo, kPiHi/Lo).
+    f32 = np.float32
+    pio2_hi, pio2_lo = f32(1.5707963705062866), f32(-4.371138828673793e-08)
+    pi_hi, pi_lo = f32(3.1415927410125732), f32(-8.742277657347586e-08)
+    assert abs(float(pio2_hi) + float(pio2_lo) - np.pi / 2) < 1e-14
+    assert abs(float(pi_hi) + float(pi_lo) - np.pi) < 1e-14
+    r = np.where(ay > ax, ((pio2_hi - r).astype(f32) + pio2_lo), r)
+    r = r.astype(f32)
+    r = np.where(x < 0, ((pi_hi - r).astype(f32) + pi_lo), r).astype(f32)
+    err = np.copysign(r, y).astype(np.float64) - np.arctan2(
+        y.astype(float), x.astype(float))
+    assert np.abs(err).max() < 4e-7
+    assert np.sqrt(np.mean(err ** 2)) < 1e-7
