@@ -169,3 +169,76 @@ def test_ctypes_structs_match_the_header(tmp_path):
         for f in py._fields_:
             assert got[(cname, f[0])] == getattr(py, f[0]).offset, \
                 (cname, f[0])
+
+
+def _bragg_desc(diamond400, mixed=False, **kw):
+    from dyfox_gb300.bragg import BraggConfig, _desc
+    from dyfox_gb300.backend import FP32, FP64
+    cfg = BraggConfig(diamond400, t_crystal=10e-6, dx=0.5e-6, half_x=8e-6)
+    d = _desc(cfg, diamond400, n_y=3, n_s=5, n_seg=1, tol=1e-10, restart=20,
+              maxiter=10, prec=FP32 if mixed else FP64)
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+def test_bragg_workspace_query_without_a_gpu(lib, diamond400):
+    """The workspace holds the couplings of every plane, the Krylov basis of
+    every (plane, s) system and, for the mixed form, the single-precision
+    and low-word copies of the couplings."""
+    from dyfox_gb300 import bragg
+    L = bragg._L()
+    d64, d32 = _bragg_desc(diamond400), _bragg_desc(diamond400, mixed=True)
+    n64, n32 = (L.dyfox_bragg_workspace_bytes(d64),
+                L.dyfox_bragg_workspace_bytes(d32))
+    plane = d64.Nz * d64.Nx
+    assert n64 >= (2 * d64.n_y * plane * 16
+                   + d64.n_y * d64.n_s * (d64.restart + 1) * d64.Nx * 16)
+    assert n32 - n64 >= 4 * d64.n_y * plane * 8
+    assert n64 % 256 == 0 and n32 % 256 == 0
+    for bad in (dict(Nx=1), dict(n_s=0), dict(tol=0.0), dict(restart=0),
+                dict(restart=2000), dict(precision=3), dict(flags=8)):
+        assert L.dyfox_bragg_workspace_bytes(
+            _bragg_desc(diamond400, **bad)) == 0, bad
+
+
+@pytest.mark.parametrize("field,value,status", [
+    ("Nx", 1, 1), ("n_y", 0, 1), ("ds", -1.0, 1), ("maxiter", 0, 1),
+    ("precision", 4, 1), ("flags", 2, 1), ("Nx", 8192, 7)])
+def test_bragg_bad_descriptors_fail_before_any_cuda_call(lib, diamond400,
+                                                         field, value, status):
+    from dyfox_gb300 import bragg
+    L = bragg._L()
+    d = _bragg_desc(diamond400, **{field: value})
+    p = ctypes.c_void_p(8)
+    st = L.dyfox_bragg_solve(d, p, p, p, None, p, None, p, 1 << 40, None)
+    assert st == status
+    assert lib.dyfox_last_error() != b""
+    assert L.dyfox_bragg_symbol(d, p, p, None, None) == status
+
+
+def test_bragg_null_pointers_modes_and_workspace(lib, diamond400):
+    from dyfox_gb300 import bragg
+    L = bragg._L()
+    p = ctypes.c_void_p(8)
+    d64, d32 = _bragg_desc(diamond400), _bragg_desc(diamond400, mixed=True)
+    n = L.dyfox_bragg_workspace_bytes(d64)
+    # NULL planes, s values, output or segment table (n_seg = 1)
+    for args in ((None, p, p, p), (p, None, p, p), (p, p, None, p),
+                 (p, p, p, None)):
+        seg, y, s, out = args
+        assert L.dyfox_bragg_solve(d64, seg, y, s, None, out, None, p, n,
+                                   None) == 1
+    assert L.dyfox_bragg_solve(d64, p, p, p, None, p, None, p, n - 1,
+                               None) == 2
+    assert L.dyfox_bragg_solve(d64, p, p, p, None, p, None, None, n,
+                               None) == 2
+    # apply: modes 0..2, the float-float march (2) only for the mixed form,
+    # the preconditioner (1) needs its input
+    for d, mode in ((d64, 3), (d64, -1), (d64, 2), (d32, 3)):
+        assert L.dyfox_bragg_apply(d, mode, p, p, p, p, p, p, p, 1 << 40,
+                                   None) == 1, (d.precision, mode)
+    assert L.dyfox_bragg_apply(d64, 1, p, p, p, None, None, p, p, 1 << 40,
+                               None) == 1
+    assert L.dyfox_bragg_symbol(d64, None, p, p, None) == 1
+    assert L.dyfox_bragg_symbol(d64, p, None, None, None) == 1
