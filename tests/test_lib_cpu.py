@@ -242,3 +242,57 @@ def test_bragg_null_pointers_modes_and_workspace(lib, diamond400):
                                None) == 1
     assert L.dyfox_bragg_symbol(d64, None, p, p, None) == 1
     assert L.dyfox_bragg_symbol(d64, p, None, None, None) == 1
+
+
+
+def test_batch_plan_without_a_gpu(lib, diamond400, small_grid):
+    """A batch of Bragg items is planned on the host alone: its workspace
+    holds every instance's own workspace and grows with each instance.
+    Bad options, NULL inputs, unknown kinds and unsupported Laue items are
+    refused before any device query."""
+    from dyfox_gb300 import batch, bragg
+    L, LB = batch._L(), bragg._L()
+    p = ctypes.c_void_p(8)
+    y = (ctypes.c_double * 3)(0.0, 1e-7, 2e-7)
+
+    def item(**kw):
+        it = batch.BatchItem()
+        it.kind = 1
+        it.bragg = _bragg_desc(diamond400, **kw)
+        it.s_dev, it.seg_table, it.out = p, p, p
+        it.y_values = ctypes.cast(y, ctypes.c_void_p)
+        return it
+
+    def plan(items, opts=None):
+        arr = (batch.BatchItem * max(len(items), 1))(*items)
+        n = ctypes.c_size_t(1)
+        st = L.dyfox_batch_workspace_bytes(arr, len(items), opts,
+                                           ctypes.byref(n))
+        return st, n.value
+
+    assert plan([]) == (0, 256)
+    one = [item()]
+    two = one + [item(mixed=True, Nz=7)]
+    st1, n1 = plan(one)
+    st2, n2 = plan(two)
+    assert st1 == 0 and st2 == 0
+    assert n1 >= LB.dyfox_bragg_workspace_bytes(one[0].bragg)
+    assert n2 - n1 >= LB.dyfox_bragg_workspace_bytes(two[1].bragg)
+    for opts in (dict(laue_cols_per_lane=6), dict(laue_warps=32),
+                 dict(laue_ctas_per_sm=-1), dict(flags=1)):
+        o = batch.BatchOpts(**opts)
+        assert plan(one, ctypes.byref(o)) == (1, 0), opts
+    no_y = item()
+    no_y.y_values = None
+    assert plan([no_y])[0] == 1
+    assert plan([item(restart=0)])[0] == 1
+    unknown = item()
+    unknown.kind = 5
+    assert plan([unknown])[0] == 1
+    # batched Laue items are single precision (here FP64: refused)
+    laue = batch.BatchItem()
+    laue.kind = 0
+    laue.laue = _desc(diamond400, small_grid)
+    laue.s_dev, laue.out = p, p
+    assert plan([laue])[0] == 7
+    assert b"DYFOX_FP32" in lib.dyfox_last_error()
