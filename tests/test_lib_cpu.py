@@ -296,3 +296,35 @@ def test_batch_plan_without_a_gpu(lib, diamond400, small_grid):
     laue.s_dev, laue.out = p, p
     assert plan([laue])[0] == 7
     assert b"DYFOX_FP32" in lib.dyfox_last_error()
+
+
+@pytest.mark.parametrize("n,Ny,Nx,prec", [
+    (0, 8, 8, 0), (1, 7, 8, 0), (1, 8, 9, 1), (1, 8, 8, 2), (2, 0, 8, 1)])
+def test_imaging_sizes_are_checked_before_any_cuda_call(lib, n, Ny, Nx,
+                                                        prec):
+    """Imaging takes even grids (the unshifted composition is exact only
+    there) and one of the two precisions."""
+    from dyfox_gb300 import optics
+    L = optics._L()
+    b = ctypes.c_size_t(1)
+    assert L.dyfox_image_workspace_bytes(n, Ny, Nx, prec,
+                                         ctypes.byref(b)) == 1
+    assert b.value == 0
+    p = ctypes.c_void_p(8)
+    assert L.dyfox_image(p, n, Ny, Nx, prec, p, p, None, None, None, None,
+                         p, 1 << 40, None) == 1
+    assert b"even" in lib.dyfox_last_error() or \
+        b"precision" in lib.dyfox_last_error()
+
+
+def test_pupil_arguments_are_checked_before_any_cuda_call(lib):
+    from dyfox_gb300 import optics
+    L = optics._L()
+    p = ctypes.c_void_p(8)
+    good = dict(Nx=8, Ny=8, dx=1e-7, f=1e-4, levels=0, prec=0, out=p)
+    for bad in (dict(Nx=0), dict(dx=0.0), dict(f=-1.0), dict(levels=-1),
+                dict(prec=3), dict(out=None)):
+        a = {**good, **bad}
+        assert L.dyfox_pupil(a["Nx"], a["Ny"], a["dx"], a["f"], 2, 0.0, 0.0,
+                             0.0, 0.0, 1, a["levels"], a["prec"], a["out"],
+                             None) == 1, bad
