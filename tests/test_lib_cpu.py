@@ -328,3 +328,23 @@ def test_pupil_arguments_are_checked_before_any_cuda_call(lib):
         assert L.dyfox_pupil(a["Nx"], a["Ny"], a["dx"], a["f"], 2, 0.0, 0.0,
                              0.0, 0.0, 1, a["levels"], a["prec"], a["out"],
                              None) == 1, bad
+
+
+def test_integration_stub_struct_matches_the_binding():
+    """The ctypes stub shown to maintainers declares dyfox_laue_desc with
+    the same fields, types and layout as the library's own binding."""
+    import re
+    from dyfox_gb300 import _lib
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    m = re.search(r"class Desc\(ctypes\.Structure\):.*?\n(\s+_fields_ = "
+                  r"\[.*?\])\n", text, re.S)
+    assert m, "no Desc struct in the stub"
+    ns = {"ctypes": ctypes, "_D": ctypes.c_double}
+    exec("class Desc(ctypes.Structure):\n" + m.group(1), ns)
+    stub = ns["Desc"]
+    assert [f[0] for f in stub._fields_] == \
+        [f[0] for f in _lib.LaueDesc._fields_]
+    assert ctypes.sizeof(stub) == ctypes.sizeof(_lib.LaueDesc)
+    for name, _ in stub._fields_:
+        assert getattr(stub, name).offset == \
+            getattr(_lib.LaueDesc, name).offset, name
