@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--once", choices=["fp32", "fp64", "bragg", "bragg32",
-                                       "scan", "image"],
+                                       "scan", "image", "batch", "unet"],
                     help="run one solve of that form after one warm-up and "
                          "exit (a small, fixed case for ncu)")
     ap.add_argument("--no-bragg", action="store_true")
@@ -280,7 +280,31 @@ def run_ours(args):
             solve_scan(bseg, bs[:4], bcfg, bys[:8], bx, bg, precision=prec)
             torch.cuda.synchronize()
         return
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    if args.once == "batch":
+        # the first 12 Laue instances of the batched-uneven set, one graph
+        from dyfox_gb300.batch import Batch, from_workload
+        from dyfox_gb300.workloads import batched_uneven
+        W = [w for w in batched_uneven() if w["kind"] == "laue"][:12]
+        b = Batch(from_workload(W), h_sum="fp64")
+        for _ in range(2):
+            b.run()
+        torch.cuda.synchronize()
+        return
+    if args.once == "unet":
+        # two training steps of the U-Net at batch 8 x 256 x 256
+        from dyfox_gb300.learned import UNet
+        torch.manual_seed(0)
+        net = UNet(batch=8, H=256, W=256, seed=3)
+        xin = (torch.randn(8, 256, 256, 32, device="cuda") * 0.5).to(
+            torch.bfloat16)
+        tgt = torch.randn(8, 256, 256, 2, device="cuda")
+        for _ in range(2):
+            net.forward(xin)
+            net.backward(tgt)
+            net.step(1e-3)
+        torch.cuda.synchronize()
+        return
+    flush =torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def timed(fn, steps, warmup):
         for _ in range(warmup):
