@@ -448,6 +448,8 @@ def run_ours(args):
         line["learned_guess"] = learned_leg(args, world)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, grid, seg, s, args.cpu_seconds)
+        line["volterra"] = volterra_leg(x, grid, seg, h_variants,
+                                        min(3.0, args.cpu_seconds))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -1187,6 +1189,53 @@ def cpu_baseline(x, grid, seg, s, seconds):
     return {"value": units / dt, "unit": "voxel-steps/s", "cores": cores,
             "kind": kind, "sample": f"{nr} of 481 active rows x {len(s)} "
             f"angles (H on those rows + FP64 march), {dt:.1f} s"}
+
+
+def volterra_leg(x, grid, seg, h_variants, seconds, max_rows=64):
+    """The Volterra phase of the README workload as the H grid (Ny, Nz, Nx)
+    that compute_H_grid builds: the GPU build in FP64 (its time from
+    ``h_variants``) beside the oracle's C restatement of the same formula
+    on all host cores, timed on blocks of ``max_rows`` central rows
+    repeated for about ``seconds``.  Unit: H evaluations (segment x voxel)
+    per second."""
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    from dyfox_gb300.grid import grid_arrays
+    from oracle import oracle as O
+    O.build()
+    geo = grid_arrays(grid)
+    Ny, Nz, Nx = geo["Ny"], geo["Nz"], geo["Nx"]
+    n_seg = len(O.segment_frames(seg, x.g_vec))
+    nr = min(Ny, max_rows)
+    rows = np.arange(Ny // 2 - nr // 2, Ny // 2 - nr // 2 + nr)
+    y = O.grid_y(Ny, geo["dx"], rows)
+
+    def block():
+        O.h_rows(seg, x.g_vec, x.nu, x.a_core, Nx, Nz, geo["dx"], geo["dz"],
+                 y)
+    block()                                   # warm-up (and page-in)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        block()
+        reps += 1
+        dt = time.perf_counter() - t0
+        if dt >= seconds:
+            break
+    units = reps * nr * Nz * Nx * n_seg
+    res = {"unit": "H evaluations/s", "grid": [Ny, Nz, Nx],
+           "segments": n_seg,
+           "cpu_baseline": {
+               "value": units / dt, "unit": "H evaluations/s",
+               "cores": O.num_threads(), "kind": "port",
+               "sample": f"{reps} x {nr} of {Ny} rows of the FP64 H grid "
+                         f"(C restatement of the Volterra formula), "
+                         f"{dt:.1f} s"}}
+    hv = (h_variants or {}).get("h_grid_f64")
+    if hv:
+        res["gpu_fp64"] = {
+            "value": Ny * Nz * Nx * n_seg / (hv["h_grid_ms"] * 1e-3),
+            "ms": hv["h_grid_ms"],
+            "form": "compute_H_grid, FP64, whole grid written to HBM"}
+    return res
 
 
 def run_reference(args):

@@ -103,3 +103,19 @@ def test_readme_workload_counts():
     assert rows == 481
     assert len(s) == 2
     assert 2 * rows * 800 * 358 == 275_516_800
+
+
+def test_volterra_leg_on_the_host():
+    """The Volterra leg's CPU baseline runs the oracle's H rows on the
+    host; the GPU rate is the whole grid's evaluations over the measured
+    FP64 grid time."""
+    import bench
+    x, grid, seg, s = bench.workload()
+    r = bench.volterra_leg(x, grid, seg, {"h_grid_f64": {"h_grid_ms": 40.0}},
+                           0.05, max_rows=2)
+    assert r["grid"] == [544, 359, 800] and r["segments"] == 1
+    cb = r["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["value"] > 0 and cb["cores"] >= 1
+    assert abs(r["gpu_fp64"]["value"] - 544 * 359 * 800 / 0.040) < 1.0
+    assert "gpu_fp64" not in bench.volterra_leg(x, grid, seg, None, 0.01,
+                                                max_rows=1)
