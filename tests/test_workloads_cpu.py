@@ -37,3 +37,46 @@ def test_batch_shape_pick_breaks_near_ties_toward_fewer_warps():
     assert pick_shape({(5, 8): 400.0, (5, 4): 420.0}) == (5, 8)
     # among equal warps, the faster
     assert pick_shape({(5, 4): 101.0, (7, 4): 100.0}) == (7, 4)
+
+
+def test_rocking_scan_configuration():
+    """544 x 1056 x 490, 256 deviation parameters over +-300 urad, 64
+    segments along signed <110> with (a/2)<110> Burgers vectors, midpoints
+    in the illuminated volume, lengths in [20, 800] um."""
+    from dyfox_gb300.units import deviation_from_urad
+    from dyfox_gb300.workloads import DIRS_110, laue_rocking_scan
+    x, grid, segs, s = laue_rocking_scan()
+    Nx, Ny, dz, ds, shift = grid.geometry()
+    assert (Ny, Nx, grid.Nz, shift) == (544, 1056, 490, 1.0)
+    assert len(s) == 256
+    assert np.allclose(s[[0, -1]], deviation_from_urad([-300.0, 300.0], x))
+    assert len(segs) == 64
+    t = grid.t_crystal
+    dirs = DIRS_110 / np.sqrt(2.0)
+    n_edge = 0
+    for ra, rb, b in segs:
+        ra, rb, b = (np.asarray(v, float) for v in (ra, rb, b))
+        L = np.linalg.norm(rb - ra)
+        assert 20e-6 * (1 - 1e-12) <= L <= 800e-6 * (1 + 1e-12)
+        xi = (rb - ra) / L
+        assert np.min(np.linalg.norm(dirs - xi, axis=1)) < 1e-12
+        assert abs(np.linalg.norm(b) - x.b_mag) < 1e-12 * x.b_mag
+        assert np.min(np.linalg.norm(dirs - b / x.b_mag, axis=1)) < 1e-12
+        n_edge += abs(np.dot(xi, b)) < 1e-12 * x.b_mag
+        c = (ra + rb) / 2
+        assert abs(c[0]) <= t * x.tan_tB and abs(c[1]) < 60e-6
+        assert 0.0 <= c[2] <= t
+    # about half pure edge by construction, plus the perpendicular draws
+    # among the "any of the 12" half
+    assert 20 <= n_edge <= 56
+
+
+def test_bragg_config1():
+    from dyfox_gb300.workloads import bragg_config1
+    x, cfg, seg, s, ys, g = bragg_config1()
+    assert (cfg.Nz, cfg.Nx) == (90, 456)
+    assert len(s) == 21 and np.isclose(s[10], 0.0, atol=1e-30)
+    assert len(ys) == 64 and np.isclose(ys[32] - ys[31], cfg.dx)
+    assert np.isclose(ys.mean(), 0.0, atol=1e-18)
+    assert len(seg) == 1
+    assert np.allclose(g[:2], 0.0) and g[2] > 0
