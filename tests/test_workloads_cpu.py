@@ -80,3 +80,28 @@ def test_bragg_config1():
     assert np.isclose(ys.mean(), 0.0, atol=1e-18)
     assert len(seg) == 1
     assert np.allclose(g[:2], 0.0) and g[2] > 0
+
+
+def test_learned_guess_instances():
+    """Thickness on the asked range (Nz 90 to 894 at dx = 0.25 um over
+    10-100 um; with half_x set by the 256-px field, Nx 648 to 3864), 256
+    planes, the field centred in the padded grid, 1-32 segments whose
+    midpoints lie within 5 um of the surface, 64 deviation parameters over
+    +-5 Darwin widths."""
+    from dyfox_gb300.bragg_geometry import BraggConfig
+    from dyfox_gb300.workloads import diamond_400, learned_guess_instances
+    x = diamond_400()
+    lo = BraggConfig(x, t_crystal=10e-6, dx=0.25e-6, half_x=32e-6)
+    hi = BraggConfig(x, t_crystal=100e-6, dx=0.25e-6, half_x=32e-6)
+    assert (lo.Nz, lo.Nx, hi.Nz, hi.Nx) == (90, 648, 894, 3864)
+    inst = learned_guess_instances(12)
+    for w in inst:
+        c = w["cfg"]
+        assert lo.Nz <= c.Nz <= hi.Nz and lo.Nx <= c.Nx <= hi.Nx
+        assert len(w["ys"]) == 256 and len(w["s"]) == 64
+        assert w["col0"] == c.Nx // 2 - 128 and w["field"] == 256
+        assert 1 <= len(w["segs"]) <= 32
+        for ra, rb, b in w["segs"]:
+            mid = (np.asarray(ra) + np.asarray(rb)) / 2
+            assert 0.0 <= mid[2] <= 5e-6 + 1e-18
+            assert abs(mid[0]) <= 32e-6 and abs(mid[1]) <= 32e-6
