@@ -11,13 +11,23 @@
 // scratch lives in one fixed-size array in the library's own device memory.
 //
 // The array is DYFOX_NOALLOC_SCRATCH_BYTES (32 MiB).  Every GPU that loads
-// the library holds it until the process exits.  Problems whose workspace
-// (dyfox_laue_workspace_bytes) is larger are rejected with DYFOX_ENOMEM.
-// Every call shares the array and the array keeps the last call's contents;
-// the solve overwrites every scratch byte it reads (per-angle tables, pivots,
-// staged phase) before reading it, so nothing has to start at zero.  Calls
-// whose work overlaps on the GPU (concurrent calls on different streams, or
-// from different host threads) race on the array: serialise them.
+// the library holds it until the process exits.  Its memory is reserved
+// when the CUDA module of this file is loaded on a device.  Under CUDA's
+// default lazy module loading that is the first call of this entry point on
+// that device (its cudaGetSymbolAddress below), so that first call can
+// still fail for lack of device memory: a caller that must never meet an
+// allocation failure mid-run makes one call during its start-up.  Under
+// eager loading (CUDA_MODULE_LOADING=EAGER) every process that loads the
+// library holds the array from the start, used or not.  Problems whose
+// workspace (dyfox_laue_workspace_bytes) is larger are rejected with
+// DYFOX_ENOMEM.  Every call shares the array and the array keeps the last
+// call's contents; the solve overwrites every scratch byte it reads
+// (per-angle tables, pivots, staged phase) before reading it, so nothing has
+// to start at zero.  Calls whose work overlaps on the GPU (concurrent calls
+// on different streams, or from different host threads) race on the array:
+// serialise them.  The array's address is looked up once per device and
+// kept; cudaDeviceReset unloads the module, so after a reset in the same
+// process this entry point must not be called again.
 #include <mutex>
 
 #include "common.cuh"

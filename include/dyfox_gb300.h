@@ -150,9 +150,15 @@ int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
  * whose dyfox_laue_workspace_bytes exceeds it return DYFOX_ENOMEM.  The
  * first call on each device looks the array's address up with that device
  * current (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls share the array, which keeps the last call's contents
- * (nothing in it has to start at zero); calls whose work overlaps on the GPU
- * race on it and must be serialised.  Allocates no device memory. */
+ * capture.  Under CUDA's default lazy module loading the array's memory is
+ * reserved at that first call on each device, which can therefore still
+ * fail for lack of device memory: callers that must not fail mid-run make
+ * one call during start-up (under CUDA_MODULE_LOADING=EAGER it is reserved
+ * when the library loads).  The address is kept for the process: do not
+ * call this entry point after a cudaDeviceReset.  All calls share the
+ * array, which keeps the last call's contents (nothing in it has to start
+ * at zero); calls whose work overlaps on the GPU race on it and must be
+ * serialised.  Later calls allocate no device memory. */
 int dyfox_laue_solve_noalloc(const dyfox_laue_desc *d, const double *s_dev,
                              const void *h_grid, const double *seg_table,
                              void *out, void *stream);

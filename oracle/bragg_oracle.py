@@ -104,15 +104,11 @@ def solve_plane(seg_list, s_dev, cfg, xtal, g_vec, y=0.0, tol=1e-10,
 
 
 def dense_solve(seg_list, s_dev, cfg, xtal, g_vec, y=0.0):
-    """Direct solve of the shooting system: exit wave and v."""
+    """Direct solve of the shooting system: exit wave and v.  The columns
+    A e_j are marched together (row j of one (Nx, Nx) march)."""
     matvec, d, H, _ = system(seg_list, s_dev, cfg, xtal, g_vec, y)
     N = cfg.Nx
-    A = np.empty((N, N), complex)
-    e = np.zeros(N, complex)
-    for j in range(N):
-        e[j] = 1.0
-        A[:, j] = matvec(e)
-        e[j] = 0.0
+    A = matvec(np.eye(N, dtype=complex)).T
     v = np.linalg.solve(A, -d)
     return v * np.exp(-1j * H[0]), v
 

@@ -107,11 +107,101 @@ def host_rows_golden():
                         cond_a=a, cond_w=wa, gh_offs=offs, gh_w=wo, **out)
 
 
+def bragg_config1_golden():
+    """The plain Bragg configuration at its own size, from the reference's
+    NumPy solver: diamond (400) at 17 keV, t = 20 um, dx = 0.5 um, half_x =
+    16 um (Nz 90, Nx 456); one edge dislocation (line [101], b = (a/2)[10-1],
+    through the column at depth t/2, half-length 800 um); 21 deviation
+    parameters evenly over +-3 Darwin widths, y-planes at (j - 32 + 1/2) dx.
+
+    Stored: ``solve_surface_batch(xp=np)`` (SciPy GMRES, tol 1e-10) on 4 of
+    the 64 planes for 3 of the 21 deviations, with its info; the perfect
+    crystal's |D_g| at the grid centre for all 21 deviations
+    (``solve_surface_batch`` of no segment, plane y = 0); and the
+    finite-thickness Riccati reflectivity at 20 um for the same
+    deviations."""
+    from bragg import (BraggConfig, bragg_g_vector, darwin_width_urad,
+                       reflectivity_riccati, solve_surface_batch)
+    from crystal import DIAMOND, CrystalParams
+    from dislocations import burgers_vector, straight_segment
+    from units import deviation_from_urad
+    x = CrystalParams.from_reflection(DIAMOND, (4, 0, 0), 17.0,
+                                      f_prime=0.003, f_dprime=0.002,
+                                      label="Diamond(400)")
+    cfg = BraggConfig(x, t_crystal=20e-6, dx=0.5e-6, half_x=16e-6)
+    g = bragg_g_vector(x)
+    b = burgers_vector(np.eye(3), [1, 0, -1], x.b_mag, +1)
+    seg = straight_segment(np.array([1.0, 0.0, 1.0]) / np.sqrt(2.0), b,
+                           [0.0, 0.0, cfg.t_crystal / 2], 800e-6)
+    w = darwin_width_urad(x)
+    urad = np.linspace(-3 * w, 3 * w, 21)
+    s_all = deviation_from_urad(urad, x)
+    ys_all = (np.arange(64) - 32 + 0.5) * cfg.dx
+    s_pick = np.array([2, 10, 17])
+    y_pick = np.array([0, 21, 32, 63])
+    surface, resid, iters = [], [], []
+    for k in s_pick:
+        out, info = solve_surface_batch(seg, float(s_all[k]), cfg,
+                                        ys_all[y_pick], x, g, xp=np)
+        assert info["converged"], info
+        surface.append(out)
+        resid.append(info["residual"])
+        iters.append(info["iterations"])
+    centre = []
+    for sd in s_all:
+        out, info = solve_surface_batch([], float(sd), cfg, np.array([0.0]),
+                                        x, g, xp=np)
+        assert info["converged"], info
+        centre.append(abs(out[0, cfg.Nx // 2]))
+    np.savez_compressed(
+        os.path.join(HERE, "bragg_cfg1.npz"),
+        cfg=np.array([20e-6, 0.5e-6, 16e-6, cfg.Nz, cfg.Nx, cfg.dz, cfg.ds]),
+        segs=np.array([np.concatenate([np.asarray(q, float)
+                                       for q in seg[0]])]),
+        g=g, urad=urad, s_dev=s_all, ys=ys_all, s_pick=s_pick,
+        y_pick=y_pick, surface=np.array(surface), residual=np.array(resid),
+        iterations=np.array(iters), pristine_centre=np.array(centre),
+        riccati_20um=reflectivity_riccati(s_all, cfg.t_crystal, x))
+
+
+def bragg_thick_golden():
+    """Where the reference's Bragg solve stops converging: one plane of a
+    100 um and of a 200 um slab (dx = 0.5 um, a 16-px field: Nz 447 / 894,
+    Nx 1852 / 3640) with 16 seeded <110> segments in the slab (the segment
+    generator of the batched configuration), s = 0.  Stored: the reference's
+    ``solve_surface_batch(xp=np)`` info with its default budget (tol 1e-10,
+    restart 40, maxiter 25, accept 1e-7)."""
+    from bragg import BraggConfig, bragg_g_vector, solve_surface_batch
+    from crystal import DIAMOND, CrystalParams
+    from dyfox_gb300.workloads import _segments_in_box
+    x = CrystalParams.from_reflection(DIAMOND, (4, 0, 0), 17.0,
+                                      f_prime=0.003, f_dprime=0.002,
+                                      label="Diamond(400)")
+    g = bragg_g_vector(x)
+    dx = 0.5e-6
+    rows = {}
+    for name, t in (("t100", 100e-6), ("t200", 200e-6)):
+        cfg = BraggConfig(x, t_crystal=t, dx=dx, half_x=16 * dx)
+        segs = _segments_in_box(x, np.random.default_rng(3), 16, 16 * dx,
+                                dx, 0.0, cfg.t_crystal)
+        _, info = solve_surface_batch(segs, 0.0, cfg, np.array([0.25 * dx]),
+                                      x, g, xp=np)
+        rows[name + "_cfg"] = np.array([t, dx, 16 * dx, cfg.Nz, cfg.Nx])
+        rows[name + "_segs"] = np.array([np.concatenate(
+            [np.asarray(q, float) for q in s]) for s in segs])
+        rows[name + "_info"] = np.array([info["residual"],
+                                         info["iterations"],
+                                         float(info["converged"])])
+    np.savez_compressed(os.path.join(HERE, "bragg_thick.npz"), y=0.25 * dx,
+                        **rows)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["optics", "host_rows"], default=None,
-                    help="write only this fixture")
+    ap.add_argument("--only", choices=["optics", "host_rows", "bragg_cfg1",
+                                       "bragg_thick"],
+                    default=None, help="write only this fixture")
     args = ap.parse_args()
     sys.dont_write_bytecode = True
     sys.path.insert(0, ROOT)
@@ -123,6 +213,14 @@ def main():
     if args.only == "host_rows":
         host_rows_golden()
         print("host_rows fixture written to", HERE)
+        return
+    if args.only == "bragg_cfg1":
+        bragg_config1_golden()
+        print("bragg_cfg1 fixture written to", HERE)
+        return
+    if args.only == "bragg_thick":
+        bragg_thick_golden()
+        print("bragg_thick fixture written to", HERE)
         return
     import subprocess
     subprocess.check_call([sys.executable, os.path.join(ROOT, "oracle",
@@ -299,6 +397,8 @@ def main():
              semi_inf=reflectivity_semi_infinite(sd_r, x))
     optics_golden()
     host_rows_golden()
+    bragg_config1_golden()
+    bragg_thick_golden()
     print("golden fixtures written to", HERE)
 
 

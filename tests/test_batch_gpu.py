@@ -163,3 +163,58 @@ def test_empty_batch(gpu):
     b = Batch([])
     b.run()
     assert b.outputs == []
+
+
+def _sample_of_the_configuration(n_laue=6, n_bragg=3, seed=4):
+    """A seeded sample of ``workloads.batched_uneven()`` (the 512-instance
+    configuration itself, not a hand-made set), limited to instances whose
+    plain-FP64 check costs seconds: Laue instances of at most 1.5e9
+    segment-voxel evaluations and 2e9 voxel-steps (316 of the 358 Laue
+    instances are under 4e9), Bragg instances of at most 5e6 voxel-steps
+    per march over all their systems."""
+    from dyfox_gb300.workloads import batched_uneven
+    inst = batched_uneven()
+    laue, bragg = [], []
+    for w in inst:
+        if w["kind"] == "laue":
+            g = w["grid"]
+            vox = g.Ny * g.Nx * g.Nz
+            if vox * len(w["segs"]) <= 1.5e9 and vox * len(w["s"]) <= 2e9:
+                laue.append(w)
+        else:
+            c = w["cfg"]
+            if c.Nx * c.Nz * len(w["ys"]) * len(w["s"]) <= 5e6:
+                bragg.append(w)
+    rng = np.random.default_rng(seed)
+    pick_l = rng.choice(len(laue), n_laue, replace=False)
+    pick_b = rng.choice(len(bragg), n_bragg, replace=False)
+    return [laue[i] for i in pick_l] + [bragg[i] for i in pick_b]
+
+
+def test_sampled_configuration_instances_match_fp64(gpu):
+    """Nine instances drawn (seeded) from the batched configuration, solved
+    in one batch in its measured form (complex64 Laue march with the H sum
+    in double, mixed-precision Bragg), each against its own plain-FP64
+    solve: Laue exit intensity <= 1e-5 relative L2; Bragg true residual
+    <= 1e-10 and exit waves <= 1e-8 relative L2."""
+    from dyfox_gb300.batch import Batch, from_workload
+    from dyfox_gb300.bragg import solve_scan
+    from dyfox_gb300.laue import solve_dislocation
+    torch = gpu
+    sample = _sample_of_the_configuration()
+    assert sum(w["kind"] == "laue" for w in sample) == 6
+    assert max(len(w["segs"]) for w in sample) > 1
+    b = Batch(from_workload(sample), h_sum="fp64")
+    b.run()
+    torch.cuda.synchronize()
+    for w, out, info in zip(sample, b.outputs, b.infos):
+        if w["kind"] == "laue":
+            ref = np_(solve_dislocation(w["segs"], w["s"], w["grid"],
+                                        w["xtal"]))
+            got = np_(out).astype(np.complex128)
+            assert rel_l2(np.abs(got) ** 2, np.abs(ref) ** 2) < 1e-5
+        else:
+            ref, rinfo = solve_scan(w["segs"], w["s"], w["cfg"], w["ys"],
+                                    w["xtal"], w["g"])
+            assert float(info[:, 0].max()) < 1e-10
+            assert rel_l2(np_(out), np_(ref)) < 1e-8

@@ -192,6 +192,71 @@ def test_fp64_matches_oracle_at_benchmark_size(gpu, diamond400, t):
     assert rel_l2(got[:, rows], want) < FP64_TOL
 
 
+def rows_clear_of_cores(segs, geo, candidates, min_px=0.05):
+    """The candidate rows on which every segment line (infinite, through the
+    segment's midpoint, as the Volterra field treats it) passes at least
+    ``min_px`` pixels from every sample node (x_i, y_row, z_k).  A core that
+    sits on a node puts atan2 at its own singularity, where two correct
+    evaluations can differ completely (reference tests/test_laue_gpu.py:
+    116-138); off the nodes the field is smooth at rounding level.
+
+    Within a row plane, a node at in-plane distance q from the line's
+    crossing point is at least q |xi_y| from the line, so the 5 x 5 nodes
+    around the crossing hold the minimum for the <110> lines (|xi_y| =
+    1/sqrt 2); a line lying in a plane y = c is |y_row - c| away."""
+    Nx, dx, dz = geo["Nx"], geo["dx"], geo["dz"]
+    keep = []
+    for r in candidates:
+        y = (r - geo["Ny"] / 2) * dx
+        dmin = np.inf
+        for ra, rb, _ in segs:
+            ra, rb = np.asarray(ra, float), np.asarray(rb, float)
+            xi = (rb - ra) / np.linalg.norm(rb - ra)
+            c = (ra + rb) / 2
+            if abs(xi[1]) < 1e-12:
+                dmin = min(dmin, abs(y - c[1]))
+                continue
+            p = c + (y - c[1]) / xi[1] * xi
+            i0 = int(np.floor(p[0] / dx + Nx / 2))
+            k0 = int(np.floor(p[2] / dz))
+            ii, kk = np.meshgrid(np.arange(i0 - 2, i0 + 3),
+                                 np.arange(k0 - 2, k0 + 3))
+            q = np.stack([(ii - Nx / 2) * dx, np.full(ii.shape, y),
+                          kk * dz], axis=-1) - c
+            dist = np.linalg.norm(np.cross(q, xi), axis=-1)
+            dmin = min(dmin, float(dist.min()))
+        if dmin >= min_px * dx:
+            keep.append(int(r))
+    return np.array(keep)
+
+
+def test_fp64_scan_of_64_segments_matches_the_oracle(gpu, diamond400):
+    """The rocking-scan configuration in plain FP64 (t = 273 um, 544 x
+    1056, Nz 490, the 64 seeded random segments): the fused Volterra phase,
+    summed over the segments in list order inside the march, against the
+    C oracle (the reference's formula and march) on six rows across the
+    beam chosen clear of every core, at the two ends and the middle of the
+    scan: <= 1e-12 relative L2."""
+    from dyfox_gb300.laue import solve_dislocation
+    from dyfox_gb300.workloads import laue_rocking_scan
+    x, grid, segs, s_all = laue_rocking_scan()
+    assert len(segs) == 64
+    s = s_all[[0, 128, 255]]
+    geo = geo_of(grid)
+    Ny = geo["Ny"]
+    half = int(grid.beam_width / 2 / geo["dx"])
+    cand = np.linspace(Ny // 2 - half + 3, Ny // 2 + half - 3, 24).astype(int)
+    rows = rows_clear_of_cores(segs, geo, cand)
+    assert len(rows) >= 6
+    rows = rows[np.linspace(0, len(rows) - 1, 6).astype(int)]
+    got = np_(solve_dislocation(segs, s, grid, x, precision="fp64"))
+    H = O.h_rows(segs, x.g_vec, x.nu, x.a_core, geo["Nx"], geo["Nz"],
+                 geo["dx"], geo["dz"], O.grid_y(Ny, geo["dx"], rows))
+    want = O.laue_march("fullfield", x, s, geo, H_rows=H, rows=rows)
+    assert np.abs(want).max() > 0
+    assert rel_l2(got[:, rows], want) < FP64_TOL
+
+
 def test_fp64_matches_the_reference_kernel_on_the_gpu(gpu, diamond400):
     """The reference's own CUDA kernel (oracle/_ref, built from its source)
     launched as laue/solver.py launches it, fed the same H grid."""

@@ -234,3 +234,31 @@ def test_single_precision_atan2_polynomial():
         y.astype(float), x.astype(float))
     assert np.abs(err).max() < 4e-7
     assert np.sqrt(np.mean(err ** 2)) < 1e-7
+
+
+def _bragg_cfg1(diamond400):
+    from dyfox_gb300.bragg_geometry import BraggConfig, bragg_g_vector
+    b = golden("bragg_cfg1")
+    t, dx, hx = b["cfg"][:3]
+    cfg = BraggConfig(diamond400, t_crystal=t, dx=dx, half_x=hx)
+    seg = [(q[:3], q[3:6], q[6:]) for q in b["segs"]]
+    return b, cfg, seg, bragg_g_vector(diamond400)
+
+
+def test_bragg_oracle_at_the_plain_bragg_configuration(diamond400):
+    """t = 20 um, dx = 0.5 um (Nz 90, Nx 456): the oracle's dense direct
+    solve against the reference's chunked SciPy GMRES answers (<= 1e-7,
+    the reference's own batched-vs-single tolerance) and its closed forms
+    against the reference's Riccati reflectivity at 20 um."""
+    from oracle import bragg_oracle as BO
+    b, cfg, seg, g = _bragg_cfg1(diamond400)
+    assert (cfg.Nz, cfg.Nx) == (90, 456)
+    s_all, ys = b["s_dev"], b["ys"]
+    for i, k in enumerate(b["s_pick"][::2]):
+        j = int(b["y_pick"][i + 1])
+        dense, _ = BO.dense_solve(seg, float(s_all[k]), cfg, diamond400, g,
+                                  y=float(ys[j]))
+        want = b["surface"][2 * i, i + 1]
+        assert np.abs(dense - want).max() < 1e-7 * np.abs(want).max()
+    got = CF.reflectivity_riccati(s_all, cfg.t_crystal, diamond400)
+    np.testing.assert_allclose(got, b["riccati_20um"], rtol=1e-9)
