@@ -66,6 +66,8 @@ _SIGNATURES = {
     "dyfox_laue_workspace_bytes": (c_size_t, [ctypes.POINTER(LaueDesc)]),
     "dyfox_pipe_peak": (c_int, [c_int, c_int, _dp, c_void_p]),
     "dyfox_launch_count": (ctypes.c_ulonglong, []),
+    "dyfox_kernel_timing": (c_int, [c_int]),
+    "dyfox_laue_kernel_ms": (c_int, [ctypes.POINTER(ctypes.c_float)]),
     "dyfox_laue_solve": (c_int, [ctypes.POINTER(LaueDesc), c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_size_t, c_void_p]),
@@ -89,6 +91,14 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def laue_kernel_ms():
+    """Durations (ms) of the prologue, staging and march kernels of the last
+    dyfox_laue_solve on this thread after ``lib().dyfox_kernel_timing(1)``."""
+    ms = (ctypes.c_float * 3)()
+    check(lib().dyfox_laue_kernel_ms(ms), "dyfox_laue_kernel_ms")
+    return [float(v) for v in ms]
 
 
 def check(status, what):

@@ -7,6 +7,8 @@
 a periodic lateral grid ``Nx = 2 (round(half_x / dx) + 2 Nz + 16)`` padded
 past the round-trip walk, and ``ds = dz / sin(theta_B)``.
 ``bragg_g_vector`` puts g along the surface normal (``geometry.py:18-20``).
+
+BraggConfig restates DYFOX's sizing rules (MIT licence: see NOTICE).
 """
 
 import numpy as np
@@ -55,34 +57,56 @@ class BraggConfig:
                 f"Nz={self.Nz}, Nx={self.Nx})")
 
 
+def _line(core, direction, half_length, burgers):
+    """One straight segment (r_start, r_end, b) centred on ``core``."""
+    core = np.asarray(core, float)
+    reach = half_length * np.asarray(direction, float)
+    return [(core - reach, core + reach, np.asarray(burgers, float))]
+
+
 def edge_segment(sign, cfg, b_mag, depth=None):
-    """Edge dislocation along y with b at 45 degrees in the (x, z) plane."""
-    depth = cfg.t_crystal * 0.25 if depth is None else depth
-    xi = np.array([0.0, 1.0, 0.0])
-    bv = sign * b_mag * np.array([1.0, 0.0, 1.0]) / np.sqrt(2.0)
-    core = np.array([0.0, 0.0, depth])
-    half = 400e-6
-    return [(core - half * xi, core + half * xi, bv)]
+    """An edge dislocation parallel to the surface, across the plane of
+    incidence: the line runs along y (half-length 400 um) through
+    (0, 0, depth), by default a quarter of the slab down; b of length
+    ``b_mag`` lies in the (x, z) plane at 45 degrees to the surface
+    normal, so g.b = |g| |b| / sqrt 2 for g along the normal (2 for
+    diamond (400)).  ``sign`` flips b (DYFOX bragg/geometry.py:69-81)."""
+    z_core = 0.25 * cfg.t_crystal if depth is None else depth
+    b = (sign * b_mag / np.sqrt(2.0)) * np.array([1.0, 0.0, 1.0])
+    return _line([0.0, 0.0, z_core], [0.0, 1.0, 0.0], 400e-6, b)
 
 
 def threading_segment(kind, sign, b_mag, g_mag, psi=np.pi / 4, y0=0.0,
                       x0=0.0, azimuth_deg=0.0):
-    """A dislocation threading the surface at ``psi`` from the normal, with
-    g.b = 2 sign for g along the normal (edge or screw)."""
-    xi = np.array([0.0, np.sin(psi), np.cos(psi)])
+    """A dislocation threading the surface at (x0, y0, 0), half-length
+    300 um (DYFOX bragg/geometry.py:83-109).
+
+    Line: tilted by ``psi`` from the surface normal towards +y, then turned
+    by ``azimuth_deg`` about the normal (out of the plane of incidence).
+    Burgers vector for g along the normal (|g| = ``g_mag``), scaled by
+    ``sign``: "Screw" -- b_mag along the line; otherwise (edge) -- the
+    normal component fixed by g.b = 2 (b_z = 2 / g_mag), the y component
+    making b normal to the untilted-in-azimuth line (b_y = -b_z / tan psi),
+    and the x component taking what is left of |b| = b_mag (zero if
+    nothing is left).  The edge vector is built for the line before the
+    azimuth turn."""
+    line = np.array([0.0, np.sin(psi), np.cos(psi)])
     if azimuth_deg:
-        c, s = np.cos(np.radians(azimuth_deg)), np.sin(np.radians(azimuth_deg))
-        xi = np.array([c * xi[0] - s * xi[1], s * xi[0] + c * xi[1], xi[2]])
-    bz = 2.0 / g_mag
+        phi = np.radians(azimuth_deg)
+        turn = np.array([[np.cos(phi), -np.sin(phi), 0.0],
+                         [np.sin(phi), np.cos(phi), 0.0],
+                         [0.0, 0.0, 1.0]])
+        line = np.array([turn[0, 0] * line[0] + turn[0, 1] * line[1],
+                         turn[1, 0] * line[0] + turn[1, 1] * line[1],
+                         line[2]])
     if kind == "Screw":
-        bv = sign * b_mag * xi
+        b = sign * b_mag * line
     else:
-        by = -bz / np.tan(psi)
-        bx = np.sqrt(max(b_mag ** 2 - bz ** 2 - by ** 2, 0.0))
-        bv = sign * np.array([bx, by, bz])
-    core = np.array([x0, y0, 0.0])
-    half = 300e-6
-    return [(core - half * xi, core + half * xi, bv)]
+        b_z = 2.0 / g_mag
+        b_y = -b_z / np.tan(psi)
+        b_x = np.sqrt(max(b_mag ** 2 - b_z ** 2 - b_y ** 2, 0.0))
+        b = sign * np.array([b_x, b_y, b_z])
+    return _line([x0, y0, 0.0], line, 300e-6, b)
 
 
 def darwin_width_urad(xtal):

@@ -12,6 +12,8 @@ as complex64 unless ``store_dtype`` says otherwise.
 
 ``solve`` returns a torch CUDA tensor (from disk on a hit, from
 ``laue.solve_dislocation`` on a miss).
+
+Restates DYFOX's WaveCache key and file format (MIT licence: see NOTICE).
 """
 
 import hashlib

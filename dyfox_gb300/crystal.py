@@ -11,6 +11,9 @@ solvers; the solvers only read attributes.
 Conventions (DYFOX ``README.md`` "Conventions" 3-4): atomic form factors
 carry ``-i f''``; ``F_0`` uses the forward factor ``Z + f' - i f''``;
 ``F_{-g} = f * conj(S_g)``.
+
+Restates DYFOX's crystal formulas and material table (MIT licence: see
+NOTICE).
 """
 
 from dataclasses import dataclass, replace

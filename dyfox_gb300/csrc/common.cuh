@@ -49,4 +49,10 @@ void launch_count_restore(unsigned long long v);
 
 inline int div_up(int a, int b) { return (a + b - 1) / b; }
 
+// Kernel timing of dyfox_laue_solve (dyfox_kernel_timing): marks 0..3 are
+// recorded on the solve's stream before the prologue, after it, after the
+// phase staging and after the march, when timing is on for the thread.
+constexpr int kLaueMarks = 4;
+void laue_mark(int slot, cudaStream_t stream);
+
 }  // namespace dyfox

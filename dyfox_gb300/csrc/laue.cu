@@ -625,6 +625,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     a.kpair = single ? (const float4 *)(ws + p.off_kpair) : nullptr;
 
     cudaError_t e;
+    laue_mark(0, stream);
     // Rows outside the beam are zero; kappa tables; pivots (one launch).
     {
         PrologueArgs pa;
@@ -659,7 +660,12 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
             if ((e = cudaGetLastError())) return cuda_status(e, "prologue");
         }
     }
-    if (p.n_rows == 0) return DYFOX_OK;
+    laue_mark(1, stream);
+    if (p.n_rows == 0) {
+        laue_mark(2, stream);
+        laue_mark(3, stream);
+        return DYFOX_OK;
+    }
     if (p.stage) {
         e = launch_cs_stage(single, (d->flags & DYFOX_FLAG_H_FP64) != 0,
                             seg_table, d->n_seg, d->Nx, d->Ny,
@@ -667,6 +673,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
                             ws + p.off_stage, stream);
         if (e) return cuda_status(e, "cs_stage");
     }
+    laue_mark(2, stream);
 
     if (p.general) {
         size_t smem = ((2 * 4 * (size_t)(d->Nx + 1) * (single ? 4 : 8) + 15) &
@@ -694,6 +701,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
             count_launch(1);
         }
         if ((e = cudaGetLastError())) return cuda_status(e, "laue_general");
+        laue_mark(3, stream);
         return DYFOX_OK;
     }
 
@@ -709,5 +717,6 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     a.raw_elem = fc.raw_elem;
     e = fc.entry.launch(a, p.n_rows * a.n_groups, fc.block, fc.smem, stream);
     if (e) return cuda_status(e, "laue_march");
+    laue_mark(3, stream);
     return DYFOX_OK;
 }

@@ -13,6 +13,8 @@ contract (the exit wave is returned on it):
   least 64); both are rounded up to multiples of 32;
 * ``ds = dz / cos(theta_B)``; ``shift_px = tan(theta_B) dz / dx`` snapped to
   the nearest integer when within 1e-9 of it.
+
+Restates DYFOX's LaueGrid sizing rules (MIT licence: see NOTICE).
 """
 
 import numpy as np

@@ -4,6 +4,8 @@ Interface and constants follow DYFOX ``units.py:13-38``: the deviation
 parameter is ``s = phi * sin(2 theta_B) / lambda`` (1/m) for a rocking angle
 ``phi`` in radians.  Crystal parameters may be given as an object with
 attributes or as a mapping.
+
+Restates DYFOX's interface and formulas (MIT licence: see NOTICE).
 """
 
 import numpy as np

@@ -398,6 +398,15 @@ int dyfox_unet_conv(int mode, const void *X, const void *G, const void *Wk,
  * `stream`; allocates one scalar of device memory for the call. */
 int dyfox_pipe_peak(int precision, int iters, double *tflops, void *stream);
 
+/* Diagnostic (not part of any DYFOX interface): with on != 0, each later
+ * dyfox_laue_solve on the calling thread records CUDA events on its stream
+ * around its kernels; dyfox_laue_kernel_ms then gives the last such solve's
+ * kernel durations in ms: [0] the prologue (zero rows, per-angle tables,
+ * pivots), [1] the e^{iH} staging (0 when not staged), [2] the march.
+ * dyfox_laue_kernel_ms synchronises on the last event. */
+int dyfox_kernel_timing(int on);
+int dyfox_laue_kernel_ms(float ms[3]);
+
 /* Number of kernels this library has launched since it was loaded. */
 unsigned long long dyfox_launch_count(void);
 

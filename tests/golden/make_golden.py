@@ -100,6 +100,23 @@ def host_rows_golden():
             x, 20e-6, 1e-4, 9, 40e-6, 7, 3e-4, **kw)
         out[name + "_S"], out[name + "_D"], out[name + "_W"] = S, D, W
         out[name + "_info"] = json.dumps(info, sort_keys=True)
+    from bragg import edge_segment, threading_segment
+
+    class _Slab:
+        t_crystal = 20e-6
+
+    built = []
+    for kind in ("Edge", "Screw"):
+        for sign in (1, -1):
+            for psi, az in ((np.pi / 4, 0.0), (0.3, 30.0), (1.1, -75.0)):
+                built.append(threading_segment(kind, sign, x.b_mag, 4.0e10,
+                                               psi, 0.3e-6, -0.2e-6, az))
+    for depth in (None, 3e-6):
+        for sign in (1, -1):
+            built.append(edge_segment(sign, _Slab, x.b_mag, depth))
+    out["builders"] = np.array([np.concatenate([np.asarray(q, float)
+                                                for q in b[0]])
+                                for b in built])
     np.savez_compressed(os.path.join(HERE, "host_rows.npz"),
                         cache_keys=np.array(keys), seg=np.array(
                             [np.concatenate([np.asarray(q, float)

@@ -46,3 +46,28 @@ def test_illumination_nodes_match_the_reference(diamond400):
         assert np.allclose(D, g[name + "_D"], rtol=1e-14, atol=0), name
         assert np.allclose(W, g[name + "_W"], rtol=1e-14, atol=0), name
         assert json.dumps(info, sort_keys=True) == str(g[name + "_info"])
+
+
+def test_bragg_segment_builders_match_the_reference(diamond400):
+    """threading_segment (edge and screw, both signs, three tilts and
+    azimuths) and edge_segment (default and given depth, both signs)
+    against the reference's builders (bragg/geometry.py:69-109)."""
+    from dyfox_gb300.bragg_geometry import edge_segment, threading_segment
+    g = golden("host_rows")
+
+    class Slab:
+        t_crystal = 20e-6
+
+    built = []
+    for kind in ("Edge", "Screw"):
+        for sign in (1, -1):
+            for psi, az in ((np.pi / 4, 0.0), (0.3, 30.0), (1.1, -75.0)):
+                built.append(threading_segment(kind, sign, diamond400.b_mag,
+                                               4.0e10, psi, 0.3e-6, -0.2e-6,
+                                               az))
+    for depth in (None, 3e-6):
+        for sign in (1, -1):
+            built.append(edge_segment(sign, Slab, diamond400.b_mag, depth))
+    got = np.array([np.concatenate([np.asarray(q, float) for q in b[0]])
+                    for b in built])
+    np.testing.assert_allclose(got, g["builders"], rtol=1e-15, atol=1e-30)
