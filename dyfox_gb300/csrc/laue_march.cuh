@@ -245,7 +245,7 @@ __device__ __forceinline__ float2 seg_phase_one(const SegF &f, float4 p0,
         __sincosf(reduce_2pi_ff(hi, e), &sn, &c);
         return make_float2(c, sn);
     } else {
-        return CS<float>::of_f64(hconst + (double)h);
+        return CS<float>::of_f64(hconst + widen_f32(h));
     }
 }
 
@@ -266,7 +266,7 @@ __device__ __forceinline__ float2 seg_phase(const SegF *segf,
     } else {
         double acc = hconst;
         for (int s = 0; s < n_seg; ++s)
-            acc += (double)h_seg_f32(segf[s], __ldg(pv + s), x);
+            acc += widen_f32(h_seg_f32(segf[s], __ldg(pv + s), x));
         return CS<float>::of_f64(acc);
     }
 }

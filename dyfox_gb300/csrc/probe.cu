@@ -3,6 +3,7 @@
 #include <atomic>
 
 #include "common.cuh"
+#include "volterra.cuh"
 
 namespace dyfox {
 
@@ -59,7 +60,39 @@ static int run_probe(int iters, double *tflops, cudaStream_t stream) {
     return DYFOX_OK;
 }
 
+// The single-precision building blocks of the fused Volterra phase beside
+// CUDA's correctly rounded operations, elementwise (dyfox_arith_probe).
+__global__ void arith_probe_kernel(int op, const float *__restrict__ a,
+                                   const float *__restrict__ b, void *out,
+                                   int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    switch (op) {
+    case 0: ((float *)out)[i] = rcp_nr(a[i]); break;
+    case 1: ((float *)out)[i] = __frcp_rn(a[i]); break;
+    case 2: ((float *)out)[i] = div_nr(a[i], b[i]); break;
+    case 3: ((float *)out)[i] = __fdiv_rn(a[i], b[i]); break;
+    case 4: ((double *)out)[i] = widen_f32(a[i]); break;
+    default: ((double *)out)[i] = (double)a[i]; break;
+    }
+}
+
 }  // namespace dyfox
+
+extern "C" int dyfox_arith_probe(int op, const float *a, const float *b,
+                                 void *out, int n, void *stream) {
+    dyfox::set_error("");
+    if (op < 0 || op > 5 || n < 0 || (n > 0 && (!a || !out)) ||
+        ((op == 2 || op == 3) && n > 0 && !b)) {
+        dyfox::set_error("bad arguments to dyfox_arith_probe");
+        return DYFOX_EINVAL;
+    }
+    if (n == 0) return DYFOX_OK;
+    dyfox::arith_probe_kernel<<<(n + 255) / 256, 256, 0,
+                                (cudaStream_t)stream>>>(op, a, b, out, n);
+    dyfox::count_launch(1);
+    return dyfox::cuda_status(cudaGetLastError(), "arith_probe");
+}
 
 extern "C" int dyfox_pipe_peak(int precision, int iters, double *tflops,
                                void *stream) {

@@ -398,6 +398,16 @@ int dyfox_unet_conv(int mode, const void *X, const void *G, const void *Wk,
  * `stream`; allocates one scalar of device memory for the call. */
 int dyfox_pipe_peak(int precision, int iters, double *tflops, void *stream);
 
+/* Diagnostic (not part of any DYFOX interface): the single-precision
+ * building blocks of the fused Volterra phase beside CUDA's correctly
+ * rounded operations, elementwise over n device floats a (and b) into out:
+ * op 0 the Newton-refined reciprocal of a, 1 __frcp_rn(a), 2 the
+ * residual-corrected quotient a / b, 3 __fdiv_rn(a, b) (float out); op 4
+ * the integer-built widening of a to double used by the FP64 segment sum,
+ * 5 the hardware conversion (double out). */
+int dyfox_arith_probe(int op, const float *a, const float *b, void *out,
+                      int n, void *stream);
+
 /* Diagnostic (not part of any DYFOX interface): with on != 0, each later
  * dyfox_laue_solve on the calling thread records CUDA events on its stream
  * around its kernels; dyfox_laue_kernel_ms then gives the last such solve's

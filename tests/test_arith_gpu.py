@@ -1,0 +1,91 @@
+"""The single-precision building blocks of the fused Volterra phase against
+CUDA's correctly rounded operations, through dyfox_arith_probe:
+
+* the Newton-refined hardware reciprocal (rcp_nr) against __frcp_rn over
+  normal x in [2^-100, 2^100], including the core clamp r2c >= a2 (pixel
+  units) of the edge terms: within 1 ulp;
+* the residual-corrected quotient (div_nr) against __fdiv_rn for
+  0 <= a <= b, the folded arguments of the atan2 polynomial: within 1 ulp;
+* the integer-built float-to-double widening of the FP64 segment sum
+  against the hardware conversion: equal bit for bit, zeros, infinities,
+  NaN and subnormals included.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _probe(torch, op, a, b=None, out_dtype=None):
+    from dyfox_gb300 import _lib
+    L = _lib.lib()
+    f = L.dyfox_arith_probe
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    at = torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+    bt = (torch.from_numpy(np.ascontiguousarray(b, np.float32)).cuda()
+          if b is not None else None)
+    out = torch.empty(len(a), dtype=out_dtype or torch.float32,
+                      device="cuda")
+    _lib.check(f(op, at.data_ptr(), bt.data_ptr() if bt is not None else
+                 None, out.data_ptr(), len(a),
+                 torch.cuda.current_stream().cuda_stream),
+               "dyfox_arith_probe")
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def _ulps(x, y):
+    """Distance in units in the last place between float32 arrays of the
+    same sign (ordered integer representations)."""
+    xi = x.view(np.int32).astype(np.int64)
+    yi = y.view(np.int32).astype(np.int64)
+    return np.abs(xi - yi)
+
+
+def test_reciprocal_within_one_ulp(gpu):
+    rng = np.random.default_rng(5)
+    x = np.exp2(rng.uniform(-100, 100, 1 << 20)).astype(np.float32)
+    # the core clamp of the edge terms: r2c >= (a_core / dx)^2, with
+    # a_core = |b| = 0.89 A and dx from 0.05 to 0.5 um
+    x[:1000] = np.float32((0.8918e-10 / 0.25e-6) ** 2) * \
+        (1 + rng.uniform(0, 4, 1000)).astype(np.float32)
+    mine = _probe(gpu, 0, x)
+    want = _probe(gpu, 1, x)
+    d = _ulps(mine, want)
+    assert d.max() <= 1
+    assert np.mean(d == 0) > 0.9
+
+
+def test_division_within_one_ulp(gpu):
+    rng = np.random.default_rng(6)
+    b = np.exp2(rng.uniform(-100, 100, 1 << 20)).astype(np.float32)
+    a = (b * rng.uniform(0, 1, b.size)).astype(np.float32)
+    a[:100] = 0.0
+    a[100:200] = b[100:200]
+    mine = _probe(gpu, 2, a, b)
+    want = _probe(gpu, 3, a, b)
+    d = _ulps(mine, want)
+    assert d.max() <= 1
+    assert np.mean(d == 0) > 0.9
+
+
+def test_widening_is_the_hardware_conversion(gpu):
+    torch = gpu
+    rng = np.random.default_rng(7)
+    bits = rng.integers(0, 1 << 32, 1 << 20, dtype=np.uint64).astype(
+        np.uint32)
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-40, -3e-45,
+                        1.17549435e-38, 3.4028235e38, 1.0, -2.5],
+                       dtype=np.float32)
+    x = np.concatenate([special, bits.view(np.float32)])
+    mine = _probe(torch, 4, x, out_dtype=torch.float64)
+    want = _probe(torch, 5, x, out_dtype=torch.float64)
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(mine), nan)
+    assert np.array_equal(mine[~nan].view(np.uint64),
+                          want[~nan].view(np.uint64))

@@ -348,3 +348,21 @@ def test_integration_stub_struct_matches_the_binding():
     for name, _ in stub._fields_:
         assert getattr(stub, name).offset == \
             getattr(_lib.LaueDesc, name).offset, name
+
+
+def test_diagnostics_refuse_bad_use_before_any_cuda_call(lib):
+    """The kernel-time read needs a timed solve on the thread first; the
+    arithmetic probe checks its operation code and pointers."""
+    import ctypes
+    from dyfox_gb300 import _lib
+    ms = (ctypes.c_float * 3)()
+    assert lib.dyfox_laue_kernel_ms(ms) == _lib.DYFOX_EINVAL
+    assert b"dyfox_kernel_timing" in lib.dyfox_last_error()
+    f = lib.dyfox_arith_probe
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    assert f(9, 8, 8, 8, 4, None) == _lib.DYFOX_EINVAL
+    assert f(2, 8, None, 8, 4, None) == _lib.DYFOX_EINVAL
+    assert f(0, None, None, 8, 4, None) == _lib.DYFOX_EINVAL
+    assert f(0, None, None, None, 0, None) == _lib.DYFOX_OK
