@@ -421,10 +421,14 @@ static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
                        FastConfig *fc) {
     const bool single = d->precision == DYFOX_FP32;
     const bool comp = single && !(d->flags & DYFOX_FLAG_NO_COMP);
-    const int ht = p.hsrc != HS_SEG ? HT_GENERIC
-                   : (single && (d->flags & DYFOX_FLAG_H_FP64)) ? HT_SEG64
-                                                                : HT_SEG;
+    const int ht_gen = p.hsrc != HS_SEG ? HT_GENERIC
+                       : (single && (d->flags & DYFOX_FLAG_H_FP64)) ? HT_SEG64
+                                                                    : HT_SEG;
     fc->pairs = use_pairs(d, p, *fc);
+    // A source staged in the march's own precision, read in place: the
+    // compile-time staged march (the pair march keeps its generic form).
+    const int ht = (ht_gen == HT_GENERIC && fc->stage == ST_DIRECT &&
+                    !fc->pairs) ? HT_STAGED : ht_gen;
     const int *cpls = fc->pairs ? kCplPair : single ? kCplF32 : kCplF64;
     const int ncpl = fc->pairs ? kNumCplPair : single ? kNumCplF32 : kNumCplF64;
     // Columns per lane: the fewest padded columns; ties go to more columns

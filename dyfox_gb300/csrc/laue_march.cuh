@@ -37,7 +37,11 @@ enum HSrc { HS_NONE = 0, HS_GRID64 = 1, HS_GRID32 = 2, HS_CS32 = 3,
 // HT_SEG sums the segment terms in float-float (two-sum) and reduces mod
 // 2 pi in single precision; HT_SEG64 sums and reduces in double.  In double
 // precision HT_SEG is the reference-order double evaluation.
-enum HTemplate { HT_GENERIC = 0, HT_SEG = 1, HT_SEG64 = 2 };
+// HT_STAGED is the march over e^{iH} staged in the march's own precision
+// (HS_CS32 single, HS_CS64 double), copied two steps ahead into a shared
+// ring: the staging mode is fixed at compile time, so the step carries no
+// branch on the source.
+enum HTemplate { HT_GENERIC = 0, HT_SEG = 1, HT_SEG64 = 2, HT_STAGED = 3 };
 
 // Interaction-picture coupling constants of one (angle, step).
 struct Kappa {
@@ -289,10 +293,17 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     const int ie_raw = grp * a.A + g;
     const int ie = ie_raw < a.n_e ? ie_raw : a.n_e - 1;
     const int Nx = a.Nx, Nz = a.Nz, nsteps = Nz - 1, ncols = a.ncols;
-    const int hsrc = HT != HT_GENERIC ? HS_SEG : a.hsrc;
-    const int stage = HT != HT_GENERIC ? (int)ST_COMPUTE : a.stage;
+    constexpr bool kSingle = sizeof(R) == 4;
+    constexpr bool kSeg = HT == HT_SEG || HT == HT_SEG64;
+    constexpr bool kStaged = HT == HT_STAGED;
+    const int hsrc = kSeg ? (int)HS_SEG
+                     : kStaged ? (kSingle ? (int)HS_CS32 : (int)HS_CS64)
+                               : a.hsrc;
+    const int stage = kSeg ? (int)ST_COMPUTE
+                      : kStaged ? (int)ST_DIRECT : a.stage;
+    const int raw_elem = kStaged ? (int)sizeof(R2) : a.raw_elem;
     const MarchSmem plan = march_smem<R>(CPL, WA, a.A, Nz, hsrc, a.n_seg,
-                                         COMP, stage, a.raw_elem);
+                                         COMP, stage, raw_elem);
     R2 *cs = reinterpret_cast<R2 *>(smem + plan.cs);
     unsigned char *raw = smem + plan.raw;
     R2 *bnd = reinterpret_cast<R2 *>(smem + plan.bnd);
@@ -301,10 +312,9 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     double *hc_sm = reinterpret_cast<double *>(smem + plan.hc);
     const int NB = COMP ? 4 : 2;
     const double y_pix = (iy - a.Ny / 2) * a.dx;
-    constexpr bool kSingle = sizeof(R) == 4;
 
     // ---------------------------------------------------------- prologue
-    if (HT != HT_GENERIC && kSingle) {
+    if (kSeg && kSingle) {
         if (tid == 0) *hc_sm = sum_hconst(a.segs, a.n_seg);
         for (int s = tid; s < a.n_seg; s += nthreads)
             segf[s] = seg_f32(a.segs + (size_t)s * DYFOX_SEG_STRIDE);
@@ -325,7 +335,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     // x = tid + i nthreads, i < nmine, all below Nx (CPL nthreads >= ncols
     // bounds nmine by CPL).  The padding columns of both buffers are zeroed
     // once here.
-    constexpr bool kFusedF32 = HT != HT_GENERIC && kSingle;
+    constexpr bool kFusedF32 = kSeg && kSingle;
     int nmine = 0;
     if constexpr (kFusedF32) {
         nmine = tid < Nx ? (Nx - 1 - tid) / nthreads + 1 : 0;
@@ -340,7 +350,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     // and that sum reduced mod 2 pi (start of the float-float sum).
     double hconst = 0.0;
     float hcr = 0.0f;
-    if (HT != HT_GENERIC && kSingle) {
+    if (kSeg && kSingle) {
         hconst = *hc_sm;
         hcr = reduce_2pi(hconst);
     }
@@ -354,12 +364,13 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         raw_src = static_cast<const unsigned char *>(grid ? a.hgrid : a.csgrid);
         raw_row = grid ? (size_t)iy * Nz : (size_t)row_blk * nsteps;
     }
-    const int chunks = (Nx * a.raw_elem) >> 4;
-    auto stage_issue = [&](int kk) {
+    const int chunks = (Nx * raw_elem) >> 4;
+    // ring: the stage (kk % 3) of step kk, tracked by the caller.
+    auto stage_issue = [&](int kk, int ring) {
         if (kk < nsteps) {
             const unsigned char *src =
-                raw_src + (raw_row + kk) * (size_t)Nx * a.raw_elem;
-            unsigned char *dst = raw + (size_t)(kk % 3) * plan.raw_stage;
+                raw_src + (raw_row + kk) * (size_t)Nx * raw_elem;
+            unsigned char *dst = raw + (size_t)ring * plan.raw_stage;
             for (int c = tid; c < chunks; c += nthreads)
                 cp_async16(dst + 16 * c, src + 16 * c);
         }
@@ -409,7 +420,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
             R2 v;
             if (x >= Nx) {
                 v.x = R(0); v.y = R(0);
-            } else if (HT != HT_GENERIC) {
+            } else if (kSeg) {
                 if constexpr (!kSingle) {
                     const double X0 = __dmul_rn((double)x - 0.5 * Nx, a.dx);
                     const double yv = __dmul_rn((double)iy - 0.5 * a.Ny, a.dx);
@@ -484,12 +495,12 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         if constexpr (COMP) { Alr[j] = 0; Ali[j] = 0; Blr[j] = 0; Bli[j] = 0; }
     }
     if (stage == ST_DIRECT) {
-        stage_issue(0);
-        stage_issue(1);
+        stage_issue(0, 0);
+        stage_issue(1, 1);
         cp_async_wait<1>();
     } else if (stage == ST_CONVERT) {
-        stage_issue(0);
-        stage_issue(1);
+        stage_issue(0, 0);
+        stage_issue(1, 1);
         cp_async_wait<0>();
         __syncthreads();
         produce(0, 0);
@@ -513,6 +524,13 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     if constexpr (kSingle) kn32 = __ldg(kap32);
     else kn = ldg_kappa(kap);
     // ------------------------------------------------------------ march
+    // Lane 31 takes A(0) of the next warp of its angle (zero past the last),
+    // lane 0 B(CPL - 1) of the previous one (zero before the first).
+    const bool is_last = lane == 31, is_first = lane == 0;
+    const bool has_next = wa + 1 < WA, has_prev = wa > 0;
+    const int nb_next = has_next ? warp + 1 : warp;
+    const int nb_prev = has_prev ? warp - 1 : warp;
+    int ring = 0, ring2 = 2;                         // k % 3, (k + 2) % 3
     for (int k = 0; k < nsteps; ++k) {
         const int p = k & 1;
         R k12r, k12i, k21r, k21i;
@@ -524,7 +542,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
             k21r = (R)kn.k21.x; k21i = (R)kn.k21.y;
             if (k + 1 < nsteps) kn = ldg_kappa(kap + k + 1);
         }
-        if (stage != ST_COMPUTE) stage_issue(k + 2);
+        if (stage != ST_COMPUTE) stage_issue(k + 2, ring2);
         if (stage != ST_DIRECT && k + 1 < nsteps) produce(k + 1, p ^ 1);
 
         // Neighbour values of the previous state.
@@ -533,40 +551,37 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         R binr = __shfl_up_sync(0xffffffffu, Br[CPL - 1], 1);
         R bini = __shfl_up_sync(0xffffffffu, Bi[CPL - 1], 1);
         R ainlr = 0, ainli = 0, binlr = 0, binli = 0;
+        (void)ainlr; (void)ainli; (void)binlr; (void)binli;
         if constexpr (COMP) {
             ainlr = __shfl_down_sync(0xffffffffu, Alr[0], 1);
             ainli = __shfl_down_sync(0xffffffffu, Ali[0], 1);
             binlr = __shfl_up_sync(0xffffffffu, Blr[CPL - 1], 1);
             binli = __shfl_up_sync(0xffffffffu, Bli[CPL - 1], 1);
         }
-        if (lane == 31) {
-            if (wa + 1 < WA) {
-                R2 t = bnd[(p * nwarps + warp + 1) * NB + 0];
-                ainr = t.x; aini = t.y;
-                if constexpr (COMP) {
-                    R2 u = bnd[(p * nwarps + warp + 1) * NB + 2];
-                    ainlr = u.x; ainli = u.y;
-                }
-            } else {
-                ainr = 0; aini = 0; ainlr = 0; ainli = 0;
-            }
-        }
-        if (lane == 0) {
-            if (wa > 0) {
-                R2 t = bnd[(p * nwarps + warp - 1) * NB + 1];
-                binr = t.x; bini = t.y;
-                if constexpr (COMP) {
-                    R2 u = bnd[(p * nwarps + warp - 1) * NB + 3];
-                    binlr = u.x; binli = u.y;
-                }
-            } else {
-                binr = 0; bini = 0; binlr = 0; binli = 0;
+        // Every lane reads the same boundary slots (a broadcast) and lanes
+        // 31 and 0 keep them by selection, with no branch.
+        {
+            const R2 t = bnd[(p * nwarps + nb_next) * NB + 0];
+            const R2 v = bnd[(p * nwarps + nb_prev) * NB + 1];
+            ainr = is_last ? (has_next ? t.x : R(0)) : ainr;
+            aini = is_last ? (has_next ? t.y : R(0)) : aini;
+            binr = is_first ? (has_prev ? v.x : R(0)) : binr;
+            bini = is_first ? (has_prev ? v.y : R(0)) : bini;
+            if constexpr (COMP) {
+                const R2 u = bnd[(p * nwarps + nb_next) * NB + 2];
+                const R2 w = bnd[(p * nwarps + nb_prev) * NB + 3];
+                ainlr = is_last ? (has_next ? u.x : R(0)) : ainlr;
+                ainli = is_last ? (has_next ? u.y : R(0)) : ainli;
+                binlr = is_first ? (has_prev ? w.x : R(0)) : binlr;
+                binli = is_first ? (has_prev ? w.y : R(0)) : binli;
             }
         }
         const R2 *src = (stage == ST_DIRECT
                              ? reinterpret_cast<const R2 *>(
-                                   raw + (size_t)(k % 3) * plan.raw_stage)
+                                   raw + (size_t)ring * plan.raw_stage)
                              : cs + (size_t)p * ncols) + L * CPL;
+        ring = ring == 2 ? 0 : ring + 1;
+        ring2 = ring2 == 2 ? 0 : ring2 + 1;
         R pbr = binr, pbi = bini, pblr = binlr, pbli = binli;
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {

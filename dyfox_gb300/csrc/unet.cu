@@ -11,8 +11,11 @@
 // in the order of the network's layer list (oracle/unet_oracle.py's
 // param_layout, the checker of these kernels).
 //
-// Every 3x3 convolution product is one implicit GEMM on the tensor cores
-// (mma.sync m16n8k16 bf16 -> f32): 64 x BN x 32 tiles, 4 warps, cp.async
+// The forward and data-gradient products run on the tcgen05 tensor cores
+// with TMEM accumulators and TMA-staged operands (unet_tc.cu) whenever the
+// image rows fit its 128-pixel tiles.  The weight gradient, and the other
+// two where the rows do not fit, are implicit GEMMs on the tensor cores
+// with mma.sync (m16n8k16 bf16 -> f32): 64 x BN x 32 tiles, 4 warps, cp.async
 // double-buffered gathers with zero fill at the image border, ldmatrix
 // (transposed where the operand is stored M- or N-contiguous):
 //   forward      C[p][co]      = sum_(t,ci) X[p+t][ci] W[co][t][ci]
@@ -27,6 +30,7 @@
 #include <new>
 
 #include "common.cuh"
+#include "unet_tc.cuh"
 
 namespace dyfox {
 
@@ -725,9 +729,24 @@ static int unet_check_shape(int batch, int H, int W) {
     return DYFOX_OK;
 }
 
-// One forward or data-gradient product (no split of K).
+// One forward or data-gradient product (no split of K): on the tcgen05
+// tensor cores when the shapes allow (unet_tc.cu), else (or with `legacy`)
+// the mma.sync implicit GEMM above.
 template <int MODE>
-static cudaError_t run_conv(const ConvArgs &a0, cudaStream_t s) {
+static cudaError_t run_conv(const ConvArgs &a0, cudaStream_t s,
+                            bool legacy = false) {
+    if (!legacy) {
+        TcConv c;
+        c.mode = MODE == CM_FWD ? 0 : 1;
+        c.act = MODE == CM_FWD ? (const void *)a0.X : (const void *)a0.G;
+        c.wk = a0.Wk;
+        c.bias = a0.bias;
+        c.out = MODE == CM_FWD ? (void *)a0.Y : (void *)a0.dX;
+        c.N = a0.N; c.H = a0.H; c.W = a0.W;
+        c.Ck = MODE == CM_FWD ? a0.Cin : a0.Cout;
+        c.Ncols = a0.Ncols;
+        if (conv_tc_supported(c)) return conv_tc_launch(c, s);
+    }
     ConvArgs a = a0;
     const int BN = a.Ncols >= 64 && a.Ncols % 64 == 0 ? 64 : 32;
     dim3 grid((a.M + kBM - 1) / kBM, (a.Ncols + BN - 1) / BN, 1);
@@ -1088,6 +1107,8 @@ extern "C" int dyfox_unet_conv(int mode, const void *X, const void *G,
         return DYFOX_EINVAL;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    const bool legacy = (mode & DYFOX_CONV_MMA_SYNC) != 0;
+    mode &= ~DYFOX_CONV_MMA_SYNC;
     ConvArgs a;
     memset(&a, 0, sizeof a);
     a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout;
@@ -1100,7 +1121,7 @@ extern "C" int dyfox_unet_conv(int mode, const void *X, const void *G,
         a.X = (const bf16 *)X; a.Wk = (const bf16 *)Wk; a.bias = bias;
         a.Y = (bf16 *)out;
         a.M = N * H * W; a.Ncols = Cout; a.K = 9 * Cin;
-        e = run_conv<CM_FWD>(a, s);
+        e = run_conv<CM_FWD>(a, s, legacy);
     } else if (mode == CM_DGRAD) {
         if (!G || !Wk || !out) {
             set_error("NULL argument");
@@ -1108,7 +1129,7 @@ extern "C" int dyfox_unet_conv(int mode, const void *X, const void *G,
         }
         a.G = (const bf16 *)G; a.Wk = (const bf16 *)Wk; a.dX = (float *)out;
         a.M = N * H * W; a.Ncols = Cin; a.K = 9 * Cout;
-        e = run_conv<CM_DGRAD>(a, s);
+        e = run_conv<CM_DGRAD>(a, s, legacy);
     } else if (mode == CM_WGRAD) {
         if (!X || !G || !out) {
             set_error("NULL argument");

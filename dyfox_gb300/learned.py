@@ -254,17 +254,22 @@ def features(h_top, col0, W, s_scaled):
     return out
 
 
-def conv(mode, *, X=None, G=None, Wk=None, bias=None, Cin=None, Cout=None):
+def conv(mode, *, X=None, G=None, Wk=None, bias=None, Cin=None, Cout=None,
+         mma_sync=False):
     """One 3x3 convolution product of the training kernels (checks):
     mode "fwd" -> bf16 relu(conv(X, Wk) + bias), "dgrad" -> float data
     gradient of G (Wk transposed [Cin][9][Cout]), "wgrad" -> float weight
-    gradient [Cout][9][Cin] of X and G.  Tensors NHWC on the GPU."""
+    gradient [Cout][9][Cin] of X and G.  Tensors NHWC on the GPU.  The
+    forward and data-gradient products run on the tcgen05 tensor cores when
+    the image rows fit its 128-pixel tiles; ``mma_sync=True`` takes the
+    mma.sync implicit GEMM instead."""
     torch = _lib.torch_cuda()
     ref = X if X is not None else G
     N, H, W = ref.shape[:3]
     Cin = Cin if Cin is not None else X.shape[3]
     Cout = Cout if Cout is not None else G.shape[3]
     m = {"fwd": 0, "dgrad": 1, "wgrad": 2}[mode]
+    flags = CONV_MMA_SYNC if mma_sync else 0
     ws = None
     if m == 0:
         out = torch.empty((N, H, W, Cout), dtype=torch.bfloat16, device="cuda")
@@ -275,11 +280,25 @@ def conv(mode, *, X=None, G=None, Wk=None, bias=None, Cin=None, Cout=None):
         ws = torch.empty(64 * 9 * Cin * Cout * 4, dtype=torch.uint8,
                          device="cuda")
     _lib.check(_L().dyfox_unet_conv(
-        m, _lib.ptr(X), _lib.ptr(G), _lib.ptr(Wk), _lib.ptr(bias),
+        m | flags, _lib.ptr(X), _lib.ptr(G), _lib.ptr(Wk), _lib.ptr(bias),
         _lib.ptr(out), N, H, W, Cin, Cout, _lib.ptr(ws),
         0 if ws is None else ws.numel(), _lib.stream_ptr()),
         "dyfox_unet_conv")
     return out
+
+
+CONV_MMA_SYNC = 16
+
+
+def tc_error(clear=True):
+    """Error code of the tcgen05 convolutions' bounded waits (0: none)."""
+    import ctypes
+    code = ctypes.c_int(0)
+    f = _L().dyfox_unet_tc_error
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.c_int]
+    _lib.check(f(ctypes.byref(code), int(bool(clear))), "dyfox_unet_tc_error")
+    return code.value
 
 
 # ---------------------------------------------------------------------------

@@ -376,6 +376,11 @@ int dyfox_unet_adam(dyfox_unet *net, float lr, float beta1, float beta2,
 int dyfox_unet_features(const double *h_top, int n_y, int Nx, int col0,
                         int W, const double *s_values, int n_s, void *x_out,
                         void *stream);
+/* Error code recorded by a tcgen05 convolution whose bounded wait expired
+ * (0 none, 1 a load, 2 a stage release, 3 the accumulator); clear != 0
+ * resets it.  Synchronises the device. */
+int dyfox_unet_tc_error(int *code, int clear);
+
 /* Device buffer of the last forward / backward pass, for checks: which 0
  * conv output `index` (bf16), 1 pooled tensor (bf16), 2 concatenated input
  * of d2a / d1a / d0a (bf16), 3 gradient of conv output `index` (float);
@@ -386,7 +391,11 @@ int dyfox_unet_buffer(dyfox_unet *net, int which, int index, void **ptr,
  * Wk) + bias)) (Wk [Cout][9][Cin]); mode 1 out = data gradient of G
  * (float, (N, H, W, Cin); Wk the transposed weights [Cin][9][Cout]); mode
  * 2 out = weight gradient [Cout][9][Cin] (float) of X and G, with the
- * split partials in the workspace.  Channels multiples of 32. */
+ * split partials in the workspace.  Channels multiples of 32.  Modes 0 and
+ * 1 run on the tcgen05 tensor cores (TMEM accumulators, TMA-staged tiles)
+ * when rows hold 128 pixels or divide 128; mode | DYFOX_CONV_MMA_SYNC runs
+ * the mma.sync implicit GEMM instead (cross-checks). */
+#define DYFOX_CONV_MMA_SYNC 16
 int dyfox_unet_conv(int mode, const void *X, const void *G, const void *Wk,
                     const float *bias, void *out, int N, int H, int W,
                     int Cin, int Cout, void *workspace,

@@ -75,6 +75,47 @@ def test_single_conv_products(gpu, rng, N, H, W, Cin, Cout):
     assert rel_l2(dw.reshape(Cout, 3, 3, Cin), dw_ref) < 1e-5
 
 
+@pytest.mark.parametrize("N,H,W,Cin,Cout", [(2, 8, 128, 32, 32),
+                                            (1, 6, 256, 32, 64),
+                                            (2, 4, 64, 64, 128),
+                                            (1, 8, 32, 128, 256),
+                                            (1, 4, 32, 384, 128)])
+def test_tcgen05_products_match_the_oracle_and_mma_sync(gpu, rng, N, H, W,
+                                                        Cin, Cout):
+    """The forward and data-gradient products on the tcgen05 tensor cores
+    (rows of 128 pixels or rows dividing 128; zero padding from the TMA
+    bounds; N split above 128 channels) against FP64 on the same bfloat16
+    operands, with the tolerances of the mma.sync products, and against the
+    mma.sync implicit GEMM itself.  No bounded wait expires."""
+    from dyfox_gb300.learned import conv, tc_error
+    torch = gpu
+    tc_error(clear=True)
+
+    def dev_bf16(a):
+        return torch.tensor(a, dtype=torch.float32).to(torch.bfloat16).cuda()
+    X = U.bf16(rng.normal(size=(N, H, W, Cin)))
+    G = U.bf16(rng.normal(size=(N, H, W, Cout)))
+    Wt = U.bf16(rng.normal(size=(Cout, 3, 3, Cin)) * 0.1)
+    b = rng.normal(size=Cout).astype(np.float32)
+    args = dict(X=dev_bf16(X), Wk=dev_bf16(Wt), bias=torch.tensor(b).cuda(),
+                Cout=Cout)
+    y = conv("fwd", **args).float().cpu().numpy()
+    y_mma = conv("fwd", mma_sync=True, **args).float().cpu().numpy()
+    ref = np.maximum(U.conv3(X, Wt, b.astype(np.float64)), 0.0)
+    assert np.all(np.abs(y - ref) <= 2.0 ** -7 * np.abs(ref) + 1e-5)
+    assert np.mean(y != U.bf16(ref)) <= 2e-3
+    assert np.mean(y != y_mma) <= 2e-3
+    dx_ref, _, _ = U.conv3_backward(X, Wt, G)
+    WtT = dev_bf16(np.ascontiguousarray(np.transpose(Wt, (3, 1, 2, 0))))
+    dx = conv("dgrad", G=dev_bf16(G), Wk=WtT, Cin=Cin,
+              Cout=Cout).cpu().numpy()
+    dx_mma = conv("dgrad", G=dev_bf16(G), Wk=WtT, Cin=Cin, Cout=Cout,
+                  mma_sync=True).cpu().numpy()
+    assert rel_l2(dx, dx_ref) < 1e-5
+    assert rel_l2(dx, dx_mma) < 1e-5
+    assert tc_error(clear=True) == 0
+
+
 def _conv_in(net, i, x, n):
     if i == 0:
         return x
