@@ -3,22 +3,30 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Workload (one "step"): the README-size Laue drop-in -- diamond (400) at
-17 keV, t = 200 um, dx = 0.25 um, beam width 120 um (grid 544 x 800,
-Nz = 359), one edge dislocation on [101] with b = (a/2)[10-1] crossing the
-beam column at t/2 (half a pixel off the sampled rows), deviation
-parameters at 0 and 117.5 urad: Volterra phase + depth march for both
-angles.  Unit: voxel-steps (angle x active row x column x depth step).
+Workload (one "step"): the rocking scan -- diamond (400) at 17 keV,
+t = 273 um, dx = 0.25 um, beam width 120 um (grid 544 x 1056, Nz = 490,
+481 illuminated rows), 64 seeded random <110> segments, 256 deviation
+parameters uniform on [-300, +300] urad: the Volterra phase of every
+voxel and the depth march of every angle, all angles in one call.
+Unit: voxel-steps (angle x active row x column x depth step).
 
---impl ours (default): the chosen form -- FP32 compensated march with the
-Volterra phase evaluated inside it (float-float segment sum, single-precision
-2 pi reduction) -- timed on the device with inputs resident; its exit intensity is checked
-against the plain FP64 form (<= 1e-5 relative L2) in the same run, and the
-plain FP64 form is timed beside it.  e2e times the public call with host
-inputs and a device-to-host read of the exit waves.
---impl reference: the reference's Laue kernel (its CUDA text compiled for the
-CPU, oracle/_ref; the oracle restatement when absent) on the host cores, on
-a bounded sample of rows per step.
+--impl ours (default): the chosen form -- FP32 march with compensated
+(Fast2Sum) amplitude updates and FP32 sincos; the segment sum of H and its
+2 pi reduction in FP64; e^{iH} evaluated once per voxel into the workspace
+and read by every angle group -- timed on the device with inputs resident.
+Its exit waves are checked against the plain FP64 form of the same scan
+(all 256 angles, timed once) in the same run: intensity within 1e-5
+relative L2, with the phase error reported.  The same march with the
+segment sum in float-float and the README-size drop-in (2 angles, one
+segment) are timed beside it.  e2e times the public call with host inputs
+and a device-to-host read of the exit waves.  reference_gpu times the
+reference's own kernel (its CUDA text, launched as DYFOX launches it) on
+the same GPU, through the reference arm below.
+--impl reference: the reference's Laue kernel (its CUDA text compiled for
+the CPU, oracle/_ref; the oracle restatement when absent) on the host cores,
+on a bounded sample of rows x angles of the same scan per step.
+--impl reference --reference-gpu: the reference's kernel on the GPU (one
+JSON object of timings; run by the ours arm as a child process).
 
 Multi-GPU: every rank runs its own replica (the path has no exchange step);
 value = all ranks' voxel-steps / max-over-ranks time.
@@ -40,14 +48,24 @@ sys.path.insert(0, ROOT)
 
 METRIC = ("voxel-steps/s (Laue scan) + Bragg solves/s at ≤1e-5 rel err, "
           "chosen vs plain FP64")
-WORKLOAD = ("laue-readme: diamond(400) 17 keV, t=200um dx=0.25um "
-            "beam_width=120um (Ny x Nx = 544 x 800, Nz=359), 1 edge "
-            "dislocation line [101] b=(a/2)[10-1] at depth t/2, "
-            "s_dev at 0 and 117.5 urad")
-# DRAM bytes (read + write) of one launch of the chosen-form march on the
-# readme workload, from the ncu capture summarised in
-# profiles/laue_march_fp32_readme.md.
-MARCH_FP32_README_DRAM_BYTES = 2843392
+WORKLOAD = ("laue-rocking-scan: diamond(400) 17 keV, t=273um dx=0.25um "
+            "beam_width=120um (Ny x Nx = 544 x 1056, Nz=490, 481 active "
+            "rows), 64 seeded random <110> segments (lengths log-uniform "
+            "20-800 um), 256 s_dev uniform on [-300, +300] urad")
+README_WORKLOAD = ("laue-readme: diamond(400) 17 keV, t=200um dx=0.25um "
+                   "beam_width=120um (Ny x Nx = 544 x 800, Nz=359), 1 edge "
+                   "dislocation line [101] b=(a/2)[10-1] at depth t/2, "
+                   "s_dev at 0 and 117.5 urad")
+# DRAM bytes (read + write) per launch of the scan's march kernel,
+# laue_march_kernel<float, 11, staged e^{iH}, compensated> with 4 angles
+# per CTA: an ncu capture of the 32-angle scan (2.13 GB: the staged e^{iH}
+# table, 1.99 GB, read once, and the exit waves) scaled to 256 angles (the
+# exit waves grow 8x, the table is read once either way).
+MARCH_SCAN_DRAM_BYTES = int(1.998e9 + 8 * 0.129e9)
+MARCH_SCAN_DRAM_SHAPE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                         "of the 32-angle scan's march launch (11 columns "
+                         "per lane, 4 angles per CTA), exit-wave writes "
+                         "scaled to 256 angles")
 
 
 def parse():
@@ -56,14 +74,20 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--reference-gpu", action="store_true",
+                    help="with --impl reference: time the reference kernel "
+                         "on the GPU and print one JSON object")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the reference-kernel-on-GPU leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--once", choices=["fp32", "fp64", "bragg", "bragg32",
-                                       "scan", "image", "batch", "unet"],
+                                       "scan", "scan256", "image", "batch",
+                                       "unet", "hgrid"],
                     help="run one solve of that form after one warm-up and "
                          "exit (a small, fixed case for ncu)")
     ap.add_argument("--no-bragg", action="store_true")
-    ap.add_argument("--no-scan", action="store_true")
+    ap.add_argument("--no-readme", action="store_true")
     ap.add_argument("--no-com-maps", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
@@ -90,6 +114,11 @@ def parse():
 
 
 def workload():
+    from dyfox_gb300.workloads import laue_rocking_scan
+    return laue_rocking_scan()
+
+
+def readme_workload():
     from dyfox_gb300.workloads import laue_readme
     return laue_readme()
 
@@ -186,12 +215,115 @@ class Clocks:
 
 
 # ------------------------------------------------------------------ ours
+def _intensity_err(a, b):
+    """Relative L2 of |a|^2 against |b|^2 (CUDA tensors, in double)."""
+    import torch
+    Ia = a.abs().double() ** 2
+    Ib = b.abs().double() ** 2
+    return float(torch.linalg.vector_norm(Ia - Ib)
+                 / torch.linalg.vector_norm(Ib))
+
+
+def _phase_err(a, b):
+    """Intensity-weighted rms phase difference (rad) of a against b."""
+    import torch
+    a = a.to(torch.complex128)
+    w = b.abs() ** 2
+    dphi = torch.angle(a * b.conj())
+    return float(torch.sqrt((w * dphi ** 2).sum() / w.sum()))
+
+
+class LaueCall:
+    """One dyfox_laue_solve through the C ABI with resident inputs and a
+    preallocated workspace and output (the autotuned shape when cached)."""
+
+    def __init__(self, x, geo, segs, s, prec, flags):
+        import torch
+        from dyfox_gb300 import _lib
+        from dyfox_gb300.autotune import lookup
+        from dyfox_gb300.laue import _desc
+        self.L = _lib.lib()
+        table = _lib.segment_table(segs, x.g_vec, x.nu, x.a_core, geo["dx"])
+        self.table = table
+        self.tdev = _lib.device_table(table)
+        self.s_dev = torch.from_numpy(np.asarray(s, float)).cuda()
+        d = _desc(x, geo, len(s), prec, _lib.H_SEGMENTS, len(table),
+                  flags=flags)
+        shape = lookup(d)
+        if shape is not None:
+            d.cols_per_lane, d.angles_per_cta, pairs = shape
+            if pairs:
+                d.flags |= _lib.FLAG_PAIRS
+        self.d = d
+        nb = self.L.dyfox_laue_workspace_bytes(d)
+        self.ws = torch.empty(max(nb, 256), dtype=torch.uint8, device="cuda")
+        self.out = torch.empty((len(s), geo["Ny"], geo["Nx"]),
+                               dtype=prec.torch_complex, device="cuda")
+        self.stream = torch.cuda.current_stream()
+
+    def __call__(self):
+        from dyfox_gb300 import _lib
+        _lib.check(self.L.dyfox_laue_solve(
+            self.d, _lib.ptr(self.s_dev), None, _lib.ptr(self.tdev),
+            _lib.ptr(self.out), _lib.ptr(self.ws), self.ws.numel(),
+            _lib.c_void_p(self.stream.cuda_stream)), "dyfox_laue_solve")
+
+
+def timed_steps(fn, steps, warmup, flush, kernel_ms=False):
+    """Device time (ms) of each of ``steps`` calls after ``warmup``, CUDA
+    events on the current stream, L2 flushed before each call outside the
+    events; with ``kernel_ms`` also each call's (prologue, staging, march)
+    kernel times from the library's events.  Returns (ms list, kernel ms
+    list, launches of this library)."""
+    import torch
+    from dyfox_gb300 import _lib
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    if kernel_ms:
+        _lib.check(L.dyfox_kernel_timing(1), "dyfox_kernel_timing")
+    ev = [(torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    km = []
+    n0 = L.dyfox_launch_count()
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        if kernel_ms:
+            km.append(_lib.laue_kernel_ms())
+    torch.cuda.synchronize()
+    launches = L.dyfox_launch_count() - n0
+    if kernel_ms:
+        _lib.check(L.dyfox_kernel_timing(0), "dyfox_kernel_timing")
+    return [a.elapsed_time(b) for a, b in ev], km, launches
+
+
+def pipe_peaks():
+    """Measured FMA throughput (TFLOP/s) of the FP32 and FP64 pipes."""
+    import ctypes
+    import torch
+    from dyfox_gb300 import _lib
+    L = _lib.lib()
+    sp = _lib.c_void_p(torch.cuda.current_stream().cuda_stream)
+    peaks = {}
+    for name, code in (("fp32", _lib.DYFOX_FP32), ("fp64", _lib.DYFOX_FP64)):
+        v = _lib.c_double(0)
+        _lib.check(L.dyfox_pipe_peak(code, 4096 if name == "fp32" else 256,
+                                     ctypes.byref(v), sp), "dyfox_pipe_peak")
+        peaks[name] = v.value
+    return peaks
+
+
 def run_ours(args):
     import torch
     from dyfox_gb300 import _lib
     from dyfox_gb300.backend import FP32, FP64
     from dyfox_gb300.grid import grid_arrays
-    from dyfox_gb300.laue import _desc, solve_dislocation
+    from dyfox_gb300.laue import solve_dislocation
 
     rank, world = dist()
     if world > 1:
@@ -199,8 +331,9 @@ def run_ours(args):
             "nccl", init_method="env://", rank=rank, world_size=world)
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    L = _lib.lib()
-    x, grid, seg, s = workload()
+    if args.once:
+        return run_once(args)
+    x, grid, segs, s = workload()
     geo = grid_arrays(grid)
     rows = active_rows(geo)
     n_e = len(s)
@@ -208,56 +341,337 @@ def run_ours(args):
     units = n_e * len(rows) * geo["Nx"] * nsteps        # voxel-steps
     voxels = len(rows) * geo["Nx"] * nsteps             # H evaluations
 
-    table = _lib.segment_table(seg, x.g_vec, x.nu, x.a_core, geo["dx"])
-    tdev = _lib.device_table(table)
-    s_dev = torch.from_numpy(np.asarray(s, float)).cuda()
-    stream = torch.cuda.current_stream()
-    sp = _lib.c_void_p(stream.cuda_stream)
-
-    from dyfox_gb300.autotune import lookup, tune
     tuned = {}
-    if not args.no_tune and not args.once:
-        for name, prec in (("fp32", FP32), ("fp64", FP64)):
-            r = tune(seg, s, grid, x, precision=prec, h_mode="fused")
-            tuned[name] = {"pairs": r.get("pairs", False),
-                           "cols_per_lane": r["cols_per_lane"],
-                           "angles_per_cta": r["angles_per_cta"]}
+    if not args.no_tune:
+        from dyfox_gb300.autotune import tune
+        for h_sum in ("fp64", "ff"):
+            r = tune(segs, s, grid, x, precision="fp32", h_mode="staged",
+                     h_sum=h_sum)
+            tuned[h_sum] = {"pairs": r.get("pairs", False),
+                            "cols_per_lane": r["cols_per_lane"],
+                            "angles_per_cta": r["angles_per_cta"]}
+    staged = _lib.FLAG_STAGED
+    chosen = LaueCall(x, geo, segs, s, FP32, staged | _lib.FLAG_H_FP64)
+    n_seg = len(chosen.table)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def make(prec, extra=0):
-        d = _desc(x, geo, n_e, prec, _lib.H_SEGMENTS, len(table),
-                  flags=_lib.FLAG_FUSED | extra)
-        shape = lookup(d)
-        if shape is not None:
-            d.cols_per_lane, d.angles_per_cta, pairs = shape
-            if pairs:
-                d.flags |= _lib.FLAG_PAIRS
-        nb = L.dyfox_laue_workspace_bytes(d)
-        ws = torch.empty(max(nb, 256), dtype=torch.uint8, device="cuda")
-        out = torch.empty((n_e, geo["Ny"], geo["Nx"]),
-                          dtype=prec.torch_complex, device="cuda")
+    peaks = pipe_peaks()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        ms, km, launches = timed_steps(chosen, args.steps, args.warmup,
+                                       flush, kernel_ms=True)
+        wall = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    tot = max_over_ranks(sum(ms) / 1e3, world)
+    value = world * units * args.steps / tot
+    mean_ms = 1e3 * tot / args.steps
+    km = np.array(km)
+    march_ms = float(km[:, 2].mean())
+    stage_ms = float(km[:, 1].mean())
+    prologue_ms = float(km[:, 0].mean())
 
-        def call():
-            _lib.check(L.dyfox_laue_solve(
-                d, _lib.ptr(s_dev), None, _lib.ptr(tdev), _lib.ptr(out),
-                _lib.ptr(ws), ws.numel(), sp), "dyfox_laue_solve")
-        return call, out
+    # The plain FP64 form of the whole scan, timed once, and the errors of
+    # the chosen form against it over all 256 angles.
+    plain = LaueCall(x, geo, segs, s, FP64, staged)
+    plain_ms, _, _ = timed_steps(plain, 1, 0, flush)
+    err_I = _intensity_err(chosen.out, plain.out)
+    err_phase = _phase_err(chosen.out, plain.out)
+    err_field = float(torch.linalg.vector_norm(
+        chosen.out.to(torch.complex128) - plain.out)
+        / torch.linalg.vector_norm(plain.out))
+    if err_I > 1e-5:
+        raise SystemExit(f"chosen form misses the 1e-5 budget: {err_I:.2e}")
+    del plain
+    torch.cuda.empty_cache()
 
-    chosen, out32 = make(FP32)
-    plain, out64 = make(FP64)
-    sum64, out32b = make(FP32, _lib.FLAG_H_FP64)
+    # The same march with the segment sum and reduction in float-float.
+    ff = LaueCall(x, geo, segs, s, FP32, staged)
+    ms_ff, km_ff, _ = timed_steps(ff, max(3, args.steps // 4), 2, flush,
+                                  kernel_ms=True)
+    ff_err = _intensity_err(ff.out, chosen.out.to(torch.complex128))
+    del ff
+
+    # e2e: the public call with host inputs (segment list, deviation
+    # parameters) and a device-to-host read of the exit waves.
+    host = torch.empty((n_e, geo["Ny"], geo["Nx"]), dtype=torch.complex64,
+                       pin_memory=True)
+    s_host = np.asarray(s, float)
+
+    def e2e():
+        o = solve_dislocation(segs, s_host, grid, x, precision=FP32,
+                              h_mode="staged", h_sum="fp64", batch=n_e)
+        host.copy_(o)
+        torch.cuda.synchronize()
+    for _ in range(2):
+        e2e()
+    ke = max(3, args.steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        e2e()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / ke, world)
+
+    # Roofline of the dominant kernel (the march): 40 flops per voxel-step
+    # (the 2 x 2 complex propagator and two complex coupling products),
+    # over the march kernel's own duration; the staging kernel beside it:
+    # 40 flops per segment-voxel of Volterra phase (atan2 and log not
+    # counted).
+    march_flops = 40.0 * units
+    stage_flops = 40.0 * n_seg * voxels
+    achieved = march_flops / (march_ms * 1e-3) / 1e12
+    stage_tf = stage_flops / (stage_ms * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": "voxel-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (compensated) + f64 H sum",
+        "data": "synthetic (seeded geometry of the benchmark configuration)",
+        "config": {"workload": WORKLOAD, "angles": n_e, "segments": n_seg,
+                   "active_rows": int(len(rows)), "Nx": geo["Nx"],
+                   "Nz": geo["Nz"], "voxel_steps_per_step": units,
+                   "form": "FP32 compensated march (Fast2Sum), FP32 sincos; "
+                           "segment sum of H and its 2 pi reduction in "
+                           "FP64; e^{iH} evaluated once per voxel into the "
+                           "workspace, all 256 angles in one call",
+                   "l2": "flushed between steps (256 MB write); the staged "
+                         "e^{iH} table (2.0 GB) and the exit waves (1.2 GB) "
+                         "exceed L2 anyway",
+                   "parallelism": f"replicas x{world}"},
+        "error_vs_fp64": {
+            "intensity_rel_l2": err_I, "field_rel_l2": err_field,
+            "phase_rms_rad_intensity_weighted": err_phase,
+            "budget_intensity": 1e-5, "angles_compared": n_e},
+        "plain_fp64": {"value": world * units / (plain_ms[0] * 1e-3),
+                       "ms_per_step": plain_ms[0], "unit": "voxel-steps/s",
+                       "form": "plain FP64 march, FP64 Volterra phase "
+                               "staged once, all 256 angles, timed once"},
+        "h_sum_float_float": {
+            "value": world * units / (statistics.mean(ms_ff) * 1e-3),
+            "ms_per_step": statistics.mean(ms_ff),
+            "stage_ms": float(np.mean([k[1] for k in km_ff])),
+            "march_ms": float(np.mean([k[2] for k in km_ff])),
+            "unit": "voxel-steps/s",
+            "intensity_rel_l2_vs_chosen": ff_err,
+            "form": "as the chosen form, segment sum and 2 pi reduction in "
+                    "float-float (two-sum) instead of FP64"},
+        "kernels_ms": {"prologue": prologue_ms, "stage": stage_ms,
+                       "march": march_ms,
+                       "source": "CUDA events of dyfox_kernel_timing around "
+                                 "each kernel of the timed calls"},
+        "e2e": {"value": world * units / e2e_s, "unit": "voxel-steps/s",
+                "ms_per_step": e2e_s * 1e3,
+                "h2d_bytes_per_step": int(8 * n_e + chosen.table.nbytes),
+                "d2h_bytes_per_step": int(host.numel() * 8),
+                "call": "solve_dislocation(segs, s_dev, grid, xtal, "
+                        "precision=FP32, h_mode='staged', h_sum='fp64', "
+                        "batch=256) + copy to pinned host memory"},
+        "roofline": {"bound": "fp32", "kernel": "laue_march_kernel",
+                     "achieved": achieved, "peak": peaks["fp32"],
+                     "unit": "TFLOP/s", "frac": achieved / peaks["fp32"],
+                     "traffic": MARCH_SCAN_DRAM_BYTES,
+                     "traffic_source": MARCH_SCAN_DRAM_SHAPE,
+                     "peak_source": "measured FFMA throughput "
+                                    "(dyfox_pipe_peak, this run); the "
+                                    "measured-peaks file has HBM and bf16 "
+                                    "figures only",
+                     "algorithmic_flops_per_launch": march_flops,
+                     "launch_ms": march_ms},
+        "stage_roofline": {"bound": "fp64 (segment sum) and fp32",
+                           "kernel": "cs_stage_kernel",
+                           "achieved": stage_tf, "peak": peaks["fp32"],
+                           "unit": "TFLOP/s",
+                           "frac": stage_tf / peaks["fp32"],
+                           "algorithmic_flops_per_launch": stage_flops,
+                           "launch_ms": stage_ms},
+        "pipe_peaks_tflops": peaks,
+        "launch_shape": {"tuned": tuned or None,
+                         "autotuner": "dyfox_gb300.autotune (cols per lane x "
+                                      "angles per CTA, each timed at about "
+                                      "2048 CTAs)"},
+        "gpu_launches": int(launches),
+        "wall_s": wall,
+    }
+    line["clocks"] = clk.summary()
+    del chosen
+    torch.cuda.empty_cache()
+    if not args.no_readme:
+        line["laue_readme"] = readme_leg(args, world, peaks)
+    if rank == 0 and world == 1 and not args.no_reference_gpu:
+        line["reference_gpu"] = reference_gpu_of_child(value, line)
+    if not args.no_bragg:
+        line["bragg"] = bragg_leg(args, rank, world, peaks)
+    if not args.no_com_maps:
+        line["com_maps"] = com_maps_leg(args, world)
+    if not args.no_batched:
+        line["batched"] = batched_leg(args, world)
+    if not args.no_learned:
+        line["learned_guess"] = learned_leg(args, world)
+        line["unet_conv"] = conv_leg()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(x, grid, segs, s,
+                                            args.cpu_seconds)
+        rx, rgrid, rseg, rs = readme_workload()
+        hv = (line.get("laue_readme") or {}).get("h_variants")
+        line["volterra"] = volterra_leg(rx, rgrid, rseg, hv,
+                                        min(3.0, args.cpu_seconds))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def reference_gpu_of_child(value, line):
+    """The reference kernel on this GPU, timed by the reference arm in a
+    child process (``--impl reference --reference-gpu``), and this arm's
+    rates over it at both Laue workloads."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl",
+           "reference", "--reference-gpu"]
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+        ref = json.loads(r.stdout.strip().splitlines()[-1])
+    except Exception as e:                      # report, do not fail
+        return {"unavailable": f"reference-kernel child failed: {e}"}
+    if "unavailable" in ref:
+        return ref
+    scan, readme = ref.get("scan", {}), ref.get("readme", {})
+    rm = line.get("laue_readme") or {}
+    out = dict(ref)
+    ratios = {}
+    for prec in ("fp64", "fp32"):
+        if prec in scan:
+            ratios[f"scan_chosen_over_ref_{prec}_march"] = \
+                value / scan[prec]["march_value"]
+            ratios[f"scan_chosen_over_ref_{prec}_with_h_grid"] = \
+                value / scan[prec]["with_h_grid_value"]
+        if prec in readme and rm.get("value"):
+            ratios[f"readme_chosen_over_ref_{prec}_march"] = \
+                rm["value"] / readme[prec]["march_value"]
+    if "fp64" in scan:
+        ratios["scan_plain_fp64_over_ref_fp64_march"] = \
+            line["plain_fp64"]["value"] / scan["fp64"]["march_value"]
+    if "fp64" in readme and rm.get("plain_fp64"):
+        ratios["readme_plain_fp64_over_ref_fp64_march"] = \
+            rm["plain_fp64"]["value"] / readme["fp64"]["march_value"]
+    out["ratio"] = ratios
+    return out
+
+
+def readme_leg(args, world, peaks):
+    """The README-size Laue drop-in (544 x 800, Nz 359, one edge
+    dislocation, 2 angles): the FP32 compensated march with the Volterra
+    phase fused into it (float-float segment sum, and the FP64 sum beside
+    it), plain FP64, e2e through solve_dislocation, and the fused phase
+    against a stored H grid (h_variants)."""
+    import torch
+    from dyfox_gb300 import _lib
+    from dyfox_gb300.backend import FP32, FP64
+    from dyfox_gb300.grid import grid_arrays
+    from dyfox_gb300.laue import solve_dislocation
+    x, grid, seg, s = readme_workload()
+    geo = grid_arrays(grid)
+    rows = active_rows(geo)
+    n_e = len(s)
+    units = n_e * len(rows) * geo["Nx"] * (geo["Nz"] - 1)
+    voxels = len(rows) * geo["Nx"] * (geo["Nz"] - 1)
+    if not args.no_tune:
+        from dyfox_gb300.autotune import tune
+        for prec in (FP32, FP64):
+            tune(seg, s, grid, x, precision=prec, h_mode="fused")
+    fused = _lib.FLAG_FUSED
+    ff = LaueCall(x, geo, seg, s, FP32, fused)
+    plain = LaueCall(x, geo, seg, s, FP64, fused)
+    sum64 = LaueCall(x, geo, seg, s, FP32, fused | _lib.FLAG_H_FP64)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ms, km, _ = timed_steps(ff, args.steps, args.warmup, flush,
+                            kernel_ms=True)
+    ms_plain, _, _ = timed_steps(plain, max(3, args.steps // 4), 2, flush)
+    ms_64, _, _ = timed_steps(sum64, max(3, args.steps // 4), 2, flush)
+    err = _intensity_err(ff.out, plain.out)
+    err64 = _intensity_err(sum64.out, plain.out)
+    t = 1e3 * max_over_ranks(statistics.mean(ms) * 1e-3, world)
+    host = torch.empty((n_e, geo["Ny"], geo["Nx"]), dtype=torch.complex64,
+                       pin_memory=True)
+
+    def e2e():
+        o = solve_dislocation(seg, np.asarray(s, float), grid, x,
+                              precision=FP32, h_mode="fused")
+        host.copy_(o)
+        torch.cuda.synchronize()
+    for _ in range(2):
+        e2e()
+    t0 = time.perf_counter()
+    ke = max(3, args.steps // 2)
+    for _ in range(ke):
+        e2e()
+    e2e_s = (time.perf_counter() - t0) / ke
+    march_ms = float(np.mean([k[2] for k in km]))
+    flops = 40.0 * units + 40.0 * len(ff.table) * voxels
+    return {
+        "value": world * units / (t * 1e-3), "unit": "voxel-steps/s",
+        "ms_per_step": t, "workload": README_WORKLOAD,
+        "voxel_steps_per_step": units,
+        "form": "FP32 compensated march, Volterra phase fused into the "
+                "march (float-float segment sum and 2 pi reduction)",
+        "intensity_rel_l2_vs_fp64": err,
+        "plain_fp64": {"value": world * units /
+                       (statistics.mean(ms_plain) * 1e-3),
+                       "ms_per_step": statistics.mean(ms_plain)},
+        "fp32_with_fp64_h_sum": {
+            "value": world * units / (statistics.mean(ms_64) * 1e-3),
+            "ms_per_step": statistics.mean(ms_64),
+            "intensity_rel_l2_vs_fp64": err64},
+        "e2e": {"value": world * units / e2e_s, "ms_per_step": e2e_s * 1e3,
+                "h2d_bytes_per_step": int(8 * n_e + ff.table.nbytes),
+                "d2h_bytes_per_step": int(host.numel() * 8)},
+        "roofline": {"bound": "fp32", "kernel": "laue_march_kernel",
+                     "achieved": flops / (march_ms * 1e-3) / 1e12,
+                     "peak": peaks["fp32"], "unit": "TFLOP/s",
+                     "frac": flops / (march_ms * 1e-3) / 1e12
+                     / peaks["fp32"],
+                     "launch_ms": march_ms,
+                     "algorithmic_flops_per_launch": flops,
+                     "note": "march and fused phase in one kernel: 40 flops "
+                             "per voxel-step + 40 per segment-voxel"},
+        "h_variants": readme_h_variants(seg, s, grid, x),
+    }
+
+
+def run_once(args):
+    """One small, fixed case of one form after one warm-up (for ncu)."""
+    import torch
+    from dyfox_gb300.backend import FP32, FP64
+    from dyfox_gb300.grid import grid_arrays
+    from dyfox_gb300.laue import solve_dislocation
     if args.once in ("fp32", "fp64"):
-        fn = chosen if args.once == "fp32" else plain
-        fn()
-        torch.cuda.synchronize()
-        fn()
-        torch.cuda.synchronize()
+        x, grid, seg, s = readme_workload()
+        geo = grid_arrays(grid)
+        from dyfox_gb300 import _lib
+        fn = LaueCall(x, geo, seg, s, FP32 if args.once == "fp32" else FP64,
+                      _lib.FLAG_FUSED)
+        for _ in range(2):
+            fn()
+            torch.cuda.synchronize()
         return
-    if args.once == "scan":
+    if args.once in ("scan", "scan256"):
         from dyfox_gb300.workloads import laue_rocking_scan
-        sx, sgrid, ssegs, ss = laue_rocking_scan(n_angles=32)
+        sx, sgrid, ssegs, ss = laue_rocking_scan(
+            n_angles=32 if args.once == "scan" else 256)
         for _ in range(2):
             solve_dislocation(ssegs, ss, sgrid, sx, precision="fp32",
-                              h_mode="staged", batch=len(ss))
+                              h_mode="staged", h_sum="fp64", batch=len(ss))
+            torch.cuda.synchronize()
+        return
+    if args.once == "hgrid":
+        from dyfox_gb300.dislocations import compute_H_grid
+        from dyfox_gb300.grid import LaueGrid
+        rx, rgrid, rseg, rs = readme_workload()
+        small = LaueGrid(rx, 100e-6, 0.25e-6, 60e-6)
+        for _ in range(2):
+            compute_H_grid(rseg, small, rx)
             torch.cuda.synchronize()
         return
     if args.once == "image":
@@ -304,156 +718,6 @@ def run_ours(args):
             net.step(1e-3)
         torch.cuda.synchronize()
         return
-    flush =torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def timed(fn, steps, warmup):
-        for _ in range(warmup):
-            fn()
-        torch.cuda.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True),
-               torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        n0 = L.dyfox_launch_count()
-        for a, b in ev:
-            flush.zero_()                 # L2 flush outside the events
-            a.record(stream)
-            fn()
-            b.record(stream)
-        torch.cuda.synchronize()
-        launches = L.dyfox_launch_count() - n0
-        return [a.elapsed_time(b) for a, b in ev], launches
-
-    # accuracy of the chosen form against plain FP64, in this run
-    chosen()
-    plain()
-    torch.cuda.synchronize()
-    I32 = out32.abs().double() ** 2
-    I64 = out64.abs() ** 2
-    err = float(torch.linalg.vector_norm(I32 - I64)
-                / torch.linalg.vector_norm(I64))
-    if err > 1e-5:
-        raise SystemExit(f"chosen form misses the 1e-5 budget: {err:.2e}")
-
-    peaks = {}
-    for name, code in (("fp32", _lib.DYFOX_FP32), ("fp64", _lib.DYFOX_FP64)):
-        v = _lib.c_double(0)
-        _lib.check(L.dyfox_pipe_peak(code, 4096 if name == "fp32" else 256,
-                                     __import__("ctypes").byref(v), sp),
-                   "dyfox_pipe_peak")
-        peaks[name] = v.value
-
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with Clocks(local) as clk:
-        t0 = time.perf_counter()
-        ms, launches = timed(chosen, args.steps, args.warmup)
-        wall = time.perf_counter() - t0
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    ms_plain, _ = timed(plain, max(3, args.steps // 4), 2)
-    ms_sum64, _ = timed(sum64, max(3, args.steps // 4), 2)
-    torch.cuda.synchronize()
-    I32b = out32b.abs().double() ** 2
-    err_sum64 = float(torch.linalg.vector_norm(I32b - I64)
-                      / torch.linalg.vector_norm(I64))
-
-    tot = max_over_ranks(sum(ms) / 1e3, world)
-    value = world * units * args.steps / tot
-    mean_ms = 1e3 * tot / args.steps
-    plain_ms = statistics.mean(ms_plain)
-
-    h_variants = None if args.once else readme_h_variants(seg, s, grid, x)
-
-    # e2e: public API, host inputs, device-to-host read of the exit waves
-    host = torch.empty((n_e, geo["Ny"], geo["Nx"]), dtype=torch.complex64,
-                       pin_memory=True)
-    s_host = np.asarray(s, float)
-
-    def e2e():
-        o = solve_dislocation(seg, s_host, grid, x, precision=FP32,
-                              h_mode="fused")
-        host.copy_(o)
-        torch.cuda.synchronize()
-    for _ in range(2):
-        e2e()
-    t0 = time.perf_counter()
-    ke = max(3, args.steps // 2)
-    for _ in range(ke):
-        e2e()
-    e2e_s = (time.perf_counter() - t0) / ke
-
-    # roofline of the march kernel: 40 flops per voxel-step (2x2 complex
-    # propagator + two complex coupling products) + 40 flops per segment-
-    # voxel of Volterra phase (atan2, log not counted)
-    flops = 40.0 * units + 40.0 * len(table) * voxels
-    achieved = flops / (mean_ms * 1e-3) / 1e12
-    line = {
-        "metric": METRIC, "value": value, "unit": "voxel-steps/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (compensated)",
-        "data": "synthetic (seeded geometry of the benchmark configuration)",
-        "config": {"workload": WORKLOAD, "angles": n_e,
-                   "active_rows": int(len(rows)), "Nx": geo["Nx"],
-                   "Nz": geo["Nz"], "voxel_steps_per_step": units,
-                   "form": "FP32 compensated march, Volterra phase fused "
-                           "(float-float segment sum and 2 pi reduction)",
-                   "l2": "flushed between steps (256 MB write)",
-                   "parallelism": f"replicas x{world}"},
-        "error_vs_fp64": {"intensity_rel_l2": err, "budget": 1e-5},
-        "plain_fp64": {"value": units / (plain_ms * 1e-3),
-                       "ms_per_step": plain_ms,
-                       "unit": "voxel-steps/s"},
-        "fp32_with_fp64_h_sum": {
-            "value": units / (statistics.mean(ms_sum64) * 1e-3),
-            "ms_per_step": statistics.mean(ms_sum64),
-            "unit": "voxel-steps/s", "intensity_rel_l2": err_sum64,
-            "form": "as the chosen form, segment sum and 2 pi reduction "
-                    "in double"},
-        "e2e": {"value": world * units / e2e_s, "unit": "voxel-steps/s",
-                "ms_per_step": e2e_s * 1e3,
-                "h2d_bytes_per_step": int(8 * n_e + table.nbytes),
-                "d2h_bytes_per_step": int(host.numel() * 8)},
-        "roofline": {"bound": "fp32", "achieved": achieved,
-                     "peak": peaks["fp32"], "unit": "TFLOP/s",
-                     "frac": achieved / peaks["fp32"],
-                     "traffic": MARCH_FP32_README_DRAM_BYTES,
-                     "traffic_source": "ncu dram__bytes_read.sum + "
-                                       "dram__bytes_write.sum of one launch "
-                                       "(profiles/laue_march_fp32_readme.md)",
-                     "peak_source": "measured FFMA throughput "
-                                    "(dyfox_pipe_peak, this run)",
-                     "algorithmic_flops_per_launch": flops},
-        "pipe_peaks_tflops": peaks,
-        "launch_shape": {"tuned": tuned or None,
-                         "autotuner": "dyfox_gb300.autotune (cols per lane x "
-                                      "angles per CTA, each timed at about "
-                                      "2048 CTAs)"},
-        "gpu_launches": int(launches),
-        "wall_s": wall,
-        "h_variants": h_variants,
-    }
-    clk_sum = clk.summary()
-    line["clocks"] = clk_sum
-    if not args.no_bragg:
-        line["bragg"] = bragg_leg(args, rank, world, peaks)
-    if not args.no_scan:
-        line["laue_scan"] = scan_leg(args, world, peaks)
-    if not args.no_com_maps:
-        line["com_maps"] = com_maps_leg(args, world)
-    if not args.no_batched:
-        line["batched"] = batched_leg(args, world)
-    if not args.no_learned:
-        line["learned_guess"] = learned_leg(args, world)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(x, grid, seg, s, args.cpu_seconds)
-        line["volterra"] = volterra_leg(x, grid, seg, h_variants,
-                                        min(3.0, args.cpu_seconds))
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
 
 
 def _fp64_row_checks(W, outs, n_streams=16):
@@ -685,6 +949,78 @@ def batched_leg(args, world):
     }
 
 
+def conv_leg(reps=20):
+    """The U-Net's widest 3x3 convolution (e0b: batch 8 x 256 x 256, 32 ->
+    32 channels) forward, and the data gradient of d2a (batch 8 x 64 x 64,
+    128 -> 384 channels), on the tcgen05 tensor cores and with the mma.sync
+    implicit GEMM, CUDA events, L2 flushed between launches.  Flops = 2 M N
+    K; bytes = the activations read and written once and the weights."""
+    import torch
+    from dyfox_gb300.learned import conv, tc_error
+    peak, src = bf16_peak()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(3)
+    res = {}
+    for name, (N, H, W, Cin, Cout, mode) in (
+            ("e0b_fwd", (8, 256, 256, 32, 32, "fwd")),
+            ("d2a_dgrad", (8, 64, 64, 384, 128, "dgrad"))):
+        if mode == "fwd":
+            X = torch.randn(N, H, W, Cin, device="cuda", generator=g).to(
+                torch.bfloat16)
+            Wk = (0.1 * torch.randn(Cout, 9, Cin, device="cuda",
+                                    generator=g)).to(torch.bfloat16)
+            b = torch.zeros(Cout, device="cuda")
+            kw = dict(X=X, Wk=Wk, bias=b, Cout=Cout)
+            Ncols, K = Cout, 9 * Cin
+            nbytes = 2 * N * H * W * (Cin + Cout) + 2 * Wk.numel()
+        else:
+            G = torch.randn(N, H, W, Cout, device="cuda", generator=g).to(
+                torch.bfloat16)
+            Wk = (0.1 * torch.randn(Cin, 9, Cout, device="cuda",
+                                    generator=g)).to(torch.bfloat16)
+            kw = dict(G=G, Wk=Wk, Cin=Cin, Cout=Cout)
+            Ncols, K = Cin, 9 * Cout
+            nbytes = 2 * N * H * W * Cout + 4 * N * H * W * Cin + \
+                2 * Wk.numel()
+        flops = 2.0 * N * H * W * Ncols * K
+        entry = {"shape_N_H_W_Cin_Cout": [N, H, W, Cin, Cout],
+                 "gflop": flops * 1e-9, "bytes": nbytes}
+        for form, mma in (("tcgen05", False), ("mma_sync", True)):
+            for _ in range(3):
+                conv(mode, mma_sync=mma, **kw)
+            ts = []
+            for _ in range(reps):
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                c = torch.cuda.Event(enable_timing=True)
+                a.record()
+                conv(mode, mma_sync=mma, **kw)
+                c.record()
+                torch.cuda.synchronize()
+                ts.append(a.elapsed_time(c))
+            ms = statistics.median(ts)
+            tf = flops / (ms * 1e-3) / 1e12
+            entry[form] = {"ms": ms, "tflops": tf, "frac_bf16_peak": tf / peak,
+                           "hbm_gbs": nbytes / (ms * 1e-3) / 1e9}
+        res[name] = entry
+    res["peak_tflops"] = peak
+    res["peak_source"] = src
+    res["tc_error"] = tc_error(clear=True)
+    return res
+
+
+def bf16_peak():
+    """(TFLOP/s, source) of the bf16 GEMM rate measured on this machine."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                        "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), \
+                "MEASURED_PEAKS.json bf16_tflops"
+    except (OSError, ValueError, KeyError):
+        return 1900.0, "fallback 1.9 PFLOP/s"
+
+
 def learned_leg(args, world):
     """Learned shooting guess (Bragg, dx 0.25 um, 256 planes x 256 px
     field, 1-32 segments within 5 um of the surface, 64 s over +-5 Darwin
@@ -807,79 +1143,6 @@ def learned_leg(args, world):
                    "solves up to --learned-tmax so that the default bench "
                    "stays within minutes",
     }
-
-
-def scan_leg(args, world, peaks=None):
-    """The 256-angle rocking scan (t = 273 um, 544 x 1056, Nz 490, 64 random
-    <110> segments): chosen FP32 form, e^{iH} staged once (float-float
-    segment sum) and read by every angle group.  Accuracy is checked
-    against plain FP64 on 8 of the 256 angles."""
-    import torch
-    from dyfox_gb300 import _lib
-    from dyfox_gb300.grid import grid_arrays
-    from dyfox_gb300.laue import solve_dislocation
-    from dyfox_gb300.workloads import laue_rocking_scan
-    x, grid, segs, s = laue_rocking_scan()
-    geo = grid_arrays(grid)
-    rows = active_rows(geo)
-    units = len(s) * len(rows) * geo["Nx"] * (geo["Nz"] - 1)
-    stream = torch.cuda.current_stream()
-    L = _lib.lib()
-    shape = None
-    if not args.no_tune:
-        from dyfox_gb300.autotune import tune
-        r = tune(segs, s, grid, x, precision="fp32", h_mode="staged")
-        shape = {"cols_per_lane": r["cols_per_lane"],
-                 "angles_per_cta": r["angles_per_cta"]}
-    for _ in range(2):
-        solve_dislocation(segs, s, grid, x, precision="fp32",
-                          h_mode="staged", batch=len(s))
-    torch.cuda.synchronize()
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    times = []
-    n0 = L.dyfox_launch_count()
-    steps = max(3, args.steps // 4)
-    for _ in range(steps):
-        flush.zero_()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        out = solve_dislocation(segs, s, grid, x, precision="fp32",
-                                h_mode="staged", batch=len(s))
-        b.record(stream)
-        torch.cuda.synchronize()
-        times.append(a.elapsed_time(b))
-    launches = L.dyfox_launch_count() - n0
-    pick = np.linspace(0, len(s) - 1, 8).round().astype(int)
-    t0 = time.perf_counter()
-    ref = solve_dislocation(segs, s[pick], grid, x, precision="fp64")
-    torch.cuda.synchronize()
-    fp64_s = time.perf_counter() - t0
-    I32 = out[torch.as_tensor(pick, device="cuda")].abs().double() ** 2
-    I64 = ref.abs() ** 2
-    err = float(torch.linalg.vector_norm(I32 - I64)
-                / torch.linalg.vector_norm(I64))
-    ms = 1e3 * max_over_ranks(statistics.mean(times) * 1e-3, world)
-    return {"value": world * units / (ms * 1e-3), "unit": "voxel-steps/s",
-            "ms_per_scan": ms, "voxel_steps_per_scan": units,
-            "angles": len(s), "segments": len(segs), "active_rows":
-            int(len(rows)), "Nx": geo["Nx"], "Nz": geo["Nz"],
-            "form": "FP32 compensated march, e^{iH} staged once "
-                    "(float-float segment sum), all angles in one call",
-            "intensity_rel_l2_vs_fp64_8_angles": err,
-            "fp64_8_angles_s": fp64_s, "gpu_launches": int(launches),
-            "launch_shape": shape,
-            "roofline": None if not peaks else {
-                "bound": "fp32",
-                # 40 flops a voxel-step (march) and 40 a segment-voxel (the
-                # staged phase, atan2 and log not counted)
-                "achieved": world * 40.0 * (units + len(rows) * geo["Nx"] *
-                                            (geo["Nz"] - 1) * len(segs))
-                / (ms * 1e-3) / 1e12,
-                "peak": peaks["fp32"], "unit": "TFLOP/s",
-                "frac": world * 40.0 * (units + len(rows) * geo["Nx"] *
-                                        (geo["Nz"] - 1) * len(segs))
-                / (ms * 1e-3) / 1e12 / peaks["fp32"]}}
 
 
 def readme_h_variants(seg, s, grid, x, reps=5):
@@ -1178,17 +1441,21 @@ def cpu_sampler(x, grid, seg, s):
 
 
 def cpu_baseline(x, grid, seg, s, seconds):
+    """The reference march on the host cores over a bounded sample of rows
+    (all angles; the (row, angle) blocks spread over the cores), sized to
+    about ``seconds``."""
     sample, kind, cores = cpu_sampler(x, grid, seg, s)
     t0 = time.perf_counter()
-    sample(cores)
-    per = (time.perf_counter() - t0) / cores
-    nr = int(max(cores, min(481, seconds / max(per, 1e-6))))
+    sample(2)
+    per = (time.perf_counter() - t0) / 2
+    nr = int(max(2, min(481, seconds / max(per, 1e-6))))
     t0 = time.perf_counter()
     units = sample(nr)
     dt = time.perf_counter() - t0
     return {"value": units / dt, "unit": "voxel-steps/s", "cores": cores,
             "kind": kind, "sample": f"{nr} of 481 active rows x {len(s)} "
-            f"angles (H on those rows + FP64 march), {dt:.1f} s"}
+            f"angles (H of the {len(seg)} segments on those rows + FP64 "
+            f"march), {dt:.1f} s"}
 
 
 def volterra_leg(x, grid, seg, h_variants, seconds, max_rows=64):
@@ -1242,34 +1509,108 @@ def run_reference(args):
     rank, world = dist()
     if rank != 0:
         return
-    x, grid, seg, s = workload()
-    sample, kind, cores = cpu_sampler(x, grid, seg, s)
+    if args.reference_gpu:
+        print(json.dumps(reference_gpu()), flush=True)
+        return
+    x, grid, segs, s = workload()
+    sample, kind, cores = cpu_sampler(x, grid, segs, s)
     t0 = time.perf_counter()
-    sample(cores)
-    per = (time.perf_counter() - t0) / cores
-    nr = int(max(cores, min(481, 2.0 / max(per, 1e-6))))
+    sample(2)
+    per = (time.perf_counter() - t0) / 2
+    nr = int(max(2, min(481, 4.0 / max(per, 1e-6))))
     for _ in range(args.warmup):
-        sample(cores)
+        sample(2)
     times, units = [], 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
         units = sample(nr)
         times.append(time.perf_counter() - t0)
     v = units * len(times) / sum(times)
+    smp = (f"{nr} of 481 active rows x all {len(s)} angles per step (H of "
+           f"the 64 segments on those rows + the FP64 march)")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v,
         "unit": "voxel-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_rows": nr},
+        "config": {"workload": WORKLOAD + "; sample: " + smp,
+                   "sample_rows": nr},
         "cpu_baseline": {"value": v, "unit": "voxel-steps/s", "cores": cores,
-                         "kind": kind,
-                         "sample": f"{nr} of 481 active rows x {len(s)} "
-                                   "angles per step"},
+                         "kind": kind, "sample": smp},
         "e2e": {"value": v, "unit": "voxel-steps/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
         flush=True)
+
+
+def reference_gpu(reps_small=5):
+    """The reference's own Laue kernel on this GPU: its CUDA text
+    (tt3d_fullfield_batch, built by oracle/make_ref.py into oracle/_ref)
+    launched as DYFOX's solve_dislocation launches it (laue/solver.py:62-90:
+    64 angles a launch, grid Ny x angles, 256 threads, planar output packed
+    into complex), fed the H grid of this build's compute_H_grid (the
+    reference's formula; DYFOX builds it with CuPy, absent here) in the
+    launch's precision.  FP64 and FP32 at the README workload and the
+    rocking scan; CUDA events on the current stream."""
+    import torch
+    from dyfox_gb300.dislocations import compute_H_grid
+    from dyfox_gb300.grid import grid_arrays
+    from oracle import oracle as O
+    O.build_ref_gpu()
+    if O.ref_gpu() is None:
+        return {"unavailable": "the reference kernel text (oracle/_ref) was "
+                               "not generated in this checkout"}
+    stream = torch.cuda.current_stream()
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+    res = {"form": "reference tt3d_fullfield_batch, 64 angles per launch as "
+                   "laue/solver.py:62-90, H grid from compute_H_grid",
+           "unit": "voxel-steps/s"}
+    for name, wl in (("readme", readme_workload), ("scan", workload)):
+        x, grid, segs, s = wl()
+        geo = grid_arrays(grid)
+        rows = active_rows(geo)
+        n_e = len(s)
+        units = n_e * len(rows) * geo["Nx"] * (geo["Nz"] - 1)
+        entry = {"voxel_steps": units}
+        for prec in ("fp64", "fp32"):
+            fp32 = prec == "fp32"
+            reps = reps_small if name == "readme" else (1 if not fp32 else 2)
+            out = torch.empty((n_e, geo["Ny"], geo["Nx"]),
+                              dtype=torch.complex64 if fp32
+                              else torch.complex128, device="cuda")
+
+            def march(H):
+                for bs in range(0, n_e, 64):
+                    be = min(bs + 64, n_e)
+                    out[bs:be] = O.ref_gpu_laue_march(
+                        "fullfield", x, s[bs:be], geo, H_grid=H, fp32=fp32)
+            h0, h1 = ev(), ev()
+            h0.record(stream)
+            H = compute_H_grid(segs, grid, x, precision=prec)
+            h1.record(stream)
+            march(H)                                    # warm-up
+            torch.cuda.synchronize()
+            h_ms = h0.elapsed_time(h1)
+            times = []
+            for _ in range(reps):
+                a, b = ev(), ev()
+                a.record(stream)
+                march(H)
+                b.record(stream)
+                torch.cuda.synchronize()
+                times.append(a.elapsed_time(b))
+            m_ms = statistics.median(times)
+            entry[prec] = {"march_ms": m_ms, "h_grid_ms": h_ms,
+                           "march_value": units / (m_ms * 1e-3),
+                           "with_h_grid_value": units / ((m_ms + h_ms)
+                                                         * 1e-3),
+                           "reps": reps}
+            del H, out
+            torch.cuda.empty_cache()
+        res[name] = entry
+    return res
 
 
 if __name__ == "__main__":

@@ -91,12 +91,20 @@ def test_bragg_flop_count():
     assert np.isclose(mgs, 16 * Nx * np.sum(j + 1), rtol=1e-14)
 
 
-def test_readme_workload_counts():
-    """The headline workload is 544 x 800 x 359 with 481 active rows and
-    two deviation parameters: 2.76e8 active voxel-steps."""
+def test_scan_and_readme_workload_counts():
+    """The headline workload is the rocking scan, 544 x 1056 x 490 with
+    481 active rows, 64 segments and 256 deviation parameters: 6.36e10
+    active voxel-steps; the README drop-in beside it is 544 x 800 x 359
+    with two deviation parameters: 2.76e8."""
     import bench
     from dyfox_gb300.grid import grid_arrays
-    x, grid, seg, s = bench.workload()
+    x, grid, segs, s = bench.workload()
+    geo = grid_arrays(grid)
+    assert (geo["Ny"], geo["Nx"], geo["Nz"]) == (544, 1056, 490)
+    rows = len(bench.active_rows(geo))
+    assert rows == 481 and len(s) == 256 and len(segs) == 64
+    assert 256 * rows * 1056 * 489 == 63_585_460_224
+    x, grid, seg, s = bench.readme_workload()
     geo = grid_arrays(grid)
     assert (geo["Ny"], geo["Nx"], geo["Nz"]) == (544, 800, 359)
     rows = len(bench.active_rows(geo))
@@ -110,7 +118,7 @@ def test_volterra_leg_on_the_host():
     host; the GPU rate is the whole grid's evaluations over the measured
     FP64 grid time."""
     import bench
-    x, grid, seg, s = bench.workload()
+    x, grid, seg, s = bench.readme_workload()
     r = bench.volterra_leg(x, grid, seg, {"h_grid_f64": {"h_grid_ms": 40.0}},
                            0.05, max_rows=2)
     assert r["grid"] == [544, 359, 800] and r["segments"] == 1
