@@ -89,7 +89,10 @@ __global__ void fft_rows_kernel(const C *__restrict__ in, C *out, int Nx,
     extern __shared__ __align__(16) unsigned char smem[];
     C *a = reinterpret_cast<C *>(smem), *b = a + Nx;
     const size_t row = (size_t)blockIdx.x * Nx;
-    for (int x = threadIdx.x; x < Nx; x += blockDim.x) a[x] = in[row + x];
+    // The exit waves are read once: a streaming load keeps them from
+    // displacing the spectra that the next two passes reread from L2.
+    for (int x = threadIdx.x; x < Nx; x += blockDim.x)
+        a[x] = __ldcs(in + row + x);
     __syncthreads();
     C *r = fft_run<C, kBigOdd<C>>(a, b, plan, tw, false);
     for (int x = threadIdx.x; x < Nx; x += blockDim.x) out[row + x] = r[x];
@@ -159,7 +162,9 @@ __global__ void rows_intensity_kernel(const C *__restrict__ data, int n,
     const int y = blockIdx.x;
     for (int e = 0; e < n; ++e) {
         const size_t row = ((size_t)e * Ny + y) * Nx;
-        for (int x = threadIdx.x; x < Nx; x += blockDim.x) a[x] = data[row + x];
+        // The last read of this spectrum row (streaming).
+        for (int x = threadIdx.x; x < Nx; x += blockDim.x)
+            a[x] = __ldcs(data + row + x);
         __syncthreads();
         const C *r = fft_run<C, kBigOdd<C>>(a, b, plan, tw, true);
         double part = 0.0;

@@ -77,7 +77,39 @@ __global__ void arith_probe_kernel(int op, const float *__restrict__ a,
     }
 }
 
+// The double-precision building blocks of the FP64 Volterra field beside
+// CUDA's, elementwise (dyfox_arith_probe64).
+__global__ void arith_probe64_kernel(int op, const double *__restrict__ a,
+                                     const double *__restrict__ b,
+                                     double *out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    switch (op) {
+    case 0: out[i] = atan2_d(a[i], b[i]); break;
+    case 1: out[i] = atan2(a[i], b[i]); break;
+    case 2: out[i] = log_d(a[i]); break;
+    case 3: out[i] = log(a[i]); break;
+    case 4: out[i] = rcp_d(a[i]); break;
+    default: out[i] = __drcp_rn(a[i]); break;
+    }
+}
+
 }  // namespace dyfox
+
+extern "C" int dyfox_arith_probe64(int op, const double *a, const double *b,
+                                   double *out, int n, void *stream) {
+    dyfox::set_error("");
+    if (op < 0 || op > 5 || n < 0 || (n > 0 && (!a || !out)) ||
+        ((op == 0 || op == 1) && n > 0 && !b)) {
+        dyfox::set_error("bad arguments to dyfox_arith_probe64");
+        return DYFOX_EINVAL;
+    }
+    if (n == 0) return DYFOX_OK;
+    dyfox::arith_probe64_kernel<<<(n + 255) / 256, 256, 0,
+                                  (cudaStream_t)stream>>>(op, a, b, out, n);
+    dyfox::count_launch(1);
+    return dyfox::cuda_status(cudaGetLastError(), "arith_probe64");
+}
 
 extern "C" int dyfox_arith_probe(int op, const float *a, const float *b,
                                  void *out, int n, void *stream) {

@@ -416,6 +416,12 @@ int dyfox_pipe_peak(int precision, int iters, double *tflops, void *stream);
  * 5 the hardware conversion (double out). */
 int dyfox_arith_probe(int op, const float *a, const float *b, void *out,
                       int n, void *stream);
+/* The same for the double-precision blocks of the FP64 Volterra field:
+ * op 0 the table-driven atan2(a, b), 1 CUDA's atan2(a, b), 2 the
+ * table-driven log(a), 3 CUDA's log(a), 4 the Newton-refined reciprocal of
+ * a, 5 __drcp_rn(a); n device doubles a (and b) into out. */
+int dyfox_arith_probe64(int op, const double *a, const double *b,
+                        double *out, int n, void *stream);
 
 /* Diagnostic (not part of any DYFOX interface): with on != 0, each later
  * dyfox_laue_solve on the calling thread records CUDA events on its stream
