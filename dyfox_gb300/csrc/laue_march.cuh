@@ -20,7 +20,8 @@
 // Each angle owns WA warps; lane L of an angle holds the CPL contiguous
 // columns [L*CPL, (L+1)*CPL) of A and B in registers.  The one-column shift
 // moves in registers, across lanes by warp shuffle and across warps through
-// a double-buffered shared-memory boundary slot; one __syncthreads per step.
+// a shared-memory boundary slot rotated over three buffers; one
+// __syncthreads per step.
 // e^{iH(k,.)} for the row is produced once per CTA per step into a
 // double-buffered shared-memory row (all angles of the CTA share it) while
 // the previous step is consumed.
@@ -42,6 +43,12 @@ enum HSrc { HS_NONE = 0, HS_GRID64 = 1, HS_GRID32 = 2, HS_CS32 = 3,
 // ring: the staging mode is fixed at compile time, so the step carries no
 // branch on the source.
 enum HTemplate { HT_GENERIC = 0, HT_SEG = 1, HT_SEG64 = 2, HT_STAGED = 3 };
+
+// A ring index known at compile time (the unrolled staged march).
+template <int N>
+struct RingIdx {
+    __host__ __device__ constexpr operator int() const { return N; }
+};
 
 // Interaction-picture coupling constants of one (angle, step).
 struct Kappa {
@@ -205,7 +212,7 @@ __host__ __device__ inline MarchSmem march_smem(int CPL, int WA, int A,
         ? ((ncols * raw_elem + 15) & ~(size_t)15) : 0;
     off += 3 * m.raw_stage;
     m.bnd = off;
-    off += (size_t)2 * nwarps * (comp ? 4 : 2) * sizeof(R2);
+    off += (size_t)3 * nwarps * (comp ? 4 : 2) * sizeof(R2);
     off = (off + 15) & ~(size_t)15;
     m.an = off;
     if (hsrc == HS_ANALYTIC) off += (size_t)Nz * sizeof(R2);
@@ -530,8 +537,15 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     const bool has_next = wa + 1 < WA, has_prev = wa > 0;
     const int nb_next = has_next ? warp + 1 : warp;
     const int nb_prev = has_prev ? warp - 1 : warp;
-    int ring = 0, ring2 = 2;                         // k % 3, (k + 2) % 3
-    for (int k = 0; k < nsteps; ++k) {
+    // One depth step.  rc is the step's ring index k % 3 (the stage of the
+    // staged row and the boundary slot it reads): a compile-time constant
+    // in the staged march, which runs the steps unrolled by three, so that
+    // every shared-memory address of the step is a constant offset; a
+    // run-time value in the other marches.
+    auto step = [&](const int k, auto rc) {
+        const int ring = rc;
+        const int ring2 = ring == 0 ? 2 : ring - 1;      // (k + 2) % 3
+        const int nslot = ring == 2 ? 0 : ring + 1;      // (k + 1) % 3
         const int p = k & 1;
         R k12r, k12i, k21r, k21i;
         if constexpr (kSingle) {
@@ -561,15 +575,15 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         // Every lane reads the same boundary slots (a broadcast) and lanes
         // 31 and 0 keep them by selection, with no branch.
         {
-            const R2 t = bnd[(p * nwarps + nb_next) * NB + 0];
-            const R2 v = bnd[(p * nwarps + nb_prev) * NB + 1];
+            const R2 t = bnd[(ring * nwarps + nb_next) * NB + 0];
+            const R2 v = bnd[(ring * nwarps + nb_prev) * NB + 1];
             ainr = is_last ? (has_next ? t.x : R(0)) : ainr;
             aini = is_last ? (has_next ? t.y : R(0)) : aini;
             binr = is_first ? (has_prev ? v.x : R(0)) : binr;
             bini = is_first ? (has_prev ? v.y : R(0)) : bini;
             if constexpr (COMP) {
-                const R2 u = bnd[(p * nwarps + nb_next) * NB + 2];
-                const R2 w = bnd[(p * nwarps + nb_prev) * NB + 3];
+                const R2 u = bnd[(ring * nwarps + nb_next) * NB + 2];
+                const R2 w = bnd[(ring * nwarps + nb_prev) * NB + 3];
                 ainlr = is_last ? (has_next ? u.x : R(0)) : ainlr;
                 ainli = is_last ? (has_next ? u.y : R(0)) : ainli;
                 binlr = is_first ? (has_prev ? w.x : R(0)) : binlr;
@@ -580,8 +594,6 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                              ? reinterpret_cast<const R2 *>(
                                    raw + (size_t)ring * plan.raw_stage)
                              : cs + (size_t)p * ncols) + L * CPL;
-        ring = ring == 2 ? 0 : ring + 1;
-        ring2 = ring2 == 2 ? 0 : ring2 + 1;
         R pbr = binr, pbi = bini, pblr = binlr, pbli = binli;
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
@@ -624,21 +636,37 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                 Alr[j] = e0; Ali[j] = e1; Blr[j] = e2; Bli[j] = e3;
             }
         }
-        const int q = p ^ 1;
         if (lane == 0) {
-            bnd[(q * nwarps + warp) * NB + 0] = R2{Ar[0], Ai[0]};
-            if constexpr (COMP) bnd[(q * nwarps + warp) * NB + 2] = R2{Alr[0], Ali[0]};
+            bnd[(nslot * nwarps + warp) * NB + 0] = R2{Ar[0], Ai[0]};
+            if constexpr (COMP)
+                bnd[(nslot * nwarps + warp) * NB + 2] = R2{Alr[0], Ali[0]};
         }
         if (lane == 31) {
-            bnd[(q * nwarps + warp) * NB + 1] = R2{Br[CPL - 1], Bi[CPL - 1]};
+            bnd[(nslot * nwarps + warp) * NB + 1] = R2{Br[CPL - 1], Bi[CPL - 1]};
             if constexpr (COMP)
-                bnd[(q * nwarps + warp) * NB + 3] = R2{Blr[CPL - 1], Bli[CPL - 1]};
+                bnd[(nslot * nwarps + warp) * NB + 3] = R2{Blr[CPL - 1], Bli[CPL - 1]};
         }
         // The stage of step k + 1 (DIRECT) or k + 2 (CONVERT) is complete
         // and, after the barrier, visible to every thread.
         if (stage == ST_DIRECT) cp_async_wait<1>();
         else if (stage == ST_CONVERT) cp_async_wait<0>();
         __syncthreads();
+    };
+    if constexpr (kStaged) {
+        int k = 0;
+        for (; k + 3 <= nsteps; k += 3) {
+            step(k, RingIdx<0>{});
+            step(k + 1, RingIdx<1>{});
+            step(k + 2, RingIdx<2>{});
+        }
+        if (k < nsteps) step(k, RingIdx<0>{});
+        if (k + 1 < nsteps) step(k + 1, RingIdx<1>{});
+    } else {
+        int ring = 0;
+        for (int k = 0; k < nsteps; ++k) {
+            step(k, ring);
+            ring = ring == 2 ? 0 : ring + 1;
+        }
     }
     if (stage != ST_COMPUTE) cp_async_wait<0>();
 

@@ -202,7 +202,20 @@ struct ImagePlan {
     size_t csize, off_stack, off_twx, off_twy, off_rock, ws, smem_rows,
         smem_cols, smem_last;
     int CB;
+    int chunk;   // images per pass sequence
 };
+
+// Images per pass sequence: the three passes run over chunks of images
+// whose intermediate spectra (chunk x Ny x Nx) fit in 24 MB, so that the
+// spectra written by one pass are read by the next from L2 rather than
+// from HBM; chunks of equal size.
+static int image_chunk(int n, int Ny, int Nx, size_t cs) {
+    const size_t one = (size_t)Ny * Nx * cs;
+    const size_t cap = (size_t)24 << 20;
+    const int cmax = one >= cap ? 1 : (int)(cap / one);
+    const int nchunks = (n + cmax - 1) / cmax;
+    return (n + nchunks - 1) / nchunks;
+}
 
 static size_t al256o(size_t v) { return (v + 255) & ~(size_t)255; }
 
@@ -220,7 +233,8 @@ static int image_plan(int n, int Ny, int Nx, int precision, ImagePlan *p) {
     const size_t cs = precision == DYFOX_FP64 ? sizeof(double2) : sizeof(float2);
     p->csize = cs;
     size_t o = 0;
-    p->off_stack = o; o = al256o(o + (size_t)n * Ny * Nx * cs);
+    p->chunk = image_chunk(n, Ny, Nx, cs);
+    p->off_stack = o; o = al256o(o + (size_t)p->chunk * Ny * Nx * cs);
     p->off_twx = o; o = al256o(o + (size_t)Nx * cs);
     p->off_twy = o; o = al256o(o + (size_t)Ny * cs);
     p->off_rock = o; o = al256o(o + (size_t)n * Ny * sizeof(double));
@@ -281,16 +295,22 @@ static int run_image(const ImagePlan &p, const void *stack, int n, int Ny,
         (e = smem_attr(cols_pupil_kernel<C>, p.smem_cols)) ||
         (e = smem_attr(rows_intensity_kernel<C>, p.smem_last)))
         return cuda_status(e, "imaging shared memory");
-    fft_rows_kernel<C><<<n * Ny, 256, p.smem_rows, s>>>((const C *)stack, buf,
-                                                       Nx, px, twx);
     const int nblk = (Nx + p.CB - 1) / p.CB;
-    cols_pupil_kernel<C><<<n * nblk, 256, p.smem_cols, s>>>(
-        buf, Ny, Nx, p.CB, py, twy, (const C *)pupil);
     const double scale = 1.0 / ((double)Nx * Ny * (double)Nx * Ny);
-    rows_intensity_kernel<C><<<Ny, 256, p.smem_last, s>>>(
-        buf, n, Ny, Nx, px, twx, scale, (R *)img, phi, sum_wI, sum_I,
-        rock_part);
-    count_launch(3);
+    const size_t plane = (size_t)Ny * Nx;
+    // The sums take the images in order across chunks, as in one pass.
+    for (int e0 = 0; e0 < n; e0 += p.chunk) {
+        const int c = n - e0 < p.chunk ? n - e0 : p.chunk;
+        fft_rows_kernel<C><<<c * Ny, 256, p.smem_rows, s>>>(
+            (const C *)stack + e0 * plane, buf, Nx, px, twx);
+        cols_pupil_kernel<C><<<c * nblk, 256, p.smem_cols, s>>>(
+            buf, Ny, Nx, p.CB, py, twy, (const C *)pupil);
+        rows_intensity_kernel<C><<<Ny, 256, p.smem_last, s>>>(
+            buf, c, Ny, Nx, px, twx, scale,
+            img ? (R *)img + e0 * plane : nullptr, phi ? phi + e0 : nullptr,
+            sum_wI, sum_I, rock_part + (size_t)e0 * Ny);
+        count_launch(3);
+    }
     if (sum_I && rock) {
         rock_reduce_kernel<<<div_up(n, 128), 128, 0, s>>>(rock_part, n, Ny,
                                                           rock);

@@ -8,53 +8,125 @@
 
 namespace dyfox {
 
-// One thread per voxel of n_rows planes of constant y.  y_dev != NULL gives
-// the planes' y; otherwise plane r is grid row r at y = (r - Ny/2) dx.
+// H of n_rows planes of constant y.  y_dev != NULL gives the planes' y;
+// otherwise plane r is grid row r at y = (r - Ny/2) dx.  A CTA takes one
+// (plane, depth) pair at a time, its threads the columns: the pair's
+// offsets from every segment core (Y - cy, Z - cz) and their products with
+// the line direction are formed once per pair in shared memory, the column
+// coordinates once per CTA, so that a voxel's double work is the
+// column-dependent part of the field (each value rounded as the
+// reference's per-voxel evaluation rounds it).  Segments are taken in
+// tiles of `tile`; between tiles a thread keeps its columns' partial sums
+// in `out` (the same values and order as one pass).
 template <bool F32OUT>
 __global__ void h_rows_kernel(const double *__restrict__ segs, int n_seg,
-                              int Nx, int Nz, double dx, double dz,
+                              int tile, int Nx, int Nz, double dx, double dz,
                               VolterraConsts vc,
                               const double *__restrict__ y_dev, int Ny,
                               long n_rows, void *out) {
-    const long total = n_rows * Nz * (long)Nx;
-    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total;
-         idx += (long)gridDim.x * blockDim.x) {
-        const int x = (int)(idx % Nx);
-        const long t = idx / Nx;
-        const int k = (int)(t % Nz);
-        const long r = t / Nz;
-        const double X0 = __dmul_rn((double)x - 0.5 * Nx, dx);
-        const double yv = y_dev ? y_dev[r] : __dmul_rn((double)r - 0.5 * Ny, dx);
+    extern __shared__ __align__(16) double hsm[];
+    double *x0 = hsm;                  // Nx: X0 of each column
+    double *yz = hsm + Nx;             // tile x 4: Y, Z, Y xi1, Z xi2
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int x = tid; x < Nx; x += nt)
+        x0[x] = __dmul_rn((double)x - 0.5 * Nx, dx);
+    const long pairs = n_rows * (long)Nz;
+    for (long rk = blockIdx.x; rk < pairs; rk += gridDim.x) {
+        const long r = rk / Nz;
+        const int k = (int)(rk - r * Nz);
+        const double yv =
+            y_dev ? y_dev[r] : __dmul_rn((double)r - 0.5 * Ny, dx);
         const double zv = __dmul_rn((double)k, dz);
-        double acc = 0.0;
-        float accf = 0.0f;
-        for (int s = 0; s < n_seg; ++s) {
-            const double *sg = segs + (size_t)s * DYFOX_SEG_STRIDE;
-            const double h = h_seg_f64(sg, __dsub_rn(X0, __ldg(sg + SEG_CX)),
-                                       __dsub_rn(yv, __ldg(sg + SEG_CY)),
-                                       __dsub_rn(zv, __ldg(sg + SEG_CZ)), vc);
-            if (F32OUT) accf = __fadd_rn(accf, __double2float_rn(h));
-            else acc = __dadd_rn(acc, h);
+        // (one pass with no segment writes zeros)
+        for (int s0 = 0; s0 < n_seg || s0 == 0; s0 += tile) {
+            const int ns = n_seg - s0 < tile ? n_seg - s0 : tile;
+            const double *sg0 = segs + (size_t)s0 * DYFOX_SEG_STRIDE;
+            __syncthreads();           // the previous tile's readers
+            for (int s = tid; s < ns; s += nt) {
+                const double *sg = sg0 + (size_t)s * DYFOX_SEG_STRIDE;
+                const double Y = __dsub_rn(yv, __ldg(sg + SEG_CY));
+                const double Z = __dsub_rn(zv, __ldg(sg + SEG_CZ));
+                yz[4 * s] = Y;
+                yz[4 * s + 1] = Z;
+                yz[4 * s + 2] = __dmul_rn(Y, __ldg(sg + SEG_XI + 1));
+                yz[4 * s + 3] = __dmul_rn(Z, __ldg(sg + SEG_XI + 2));
+            }
+            __syncthreads();
+            for (int x = tid; x < Nx; x += nt) {
+                const double X0 = x0[x];
+                const size_t idx = (size_t)rk * Nx + x;
+                double acc = 0.0;
+                float accf = 0.0f;
+                if (s0) {
+                    if (F32OUT) accf = ((const float *)out)[idx];
+                    else acc = ((const double *)out)[idx];
+                }
+                for (int s = 0; s < ns; ++s) {
+                    const double *sg = sg0 + (size_t)s * DYFOX_SEG_STRIDE;
+                    const double h = h_seg_f64h(
+                        sg, __dsub_rn(X0, __ldg(sg + SEG_CX)), yz[4 * s],
+                        yz[4 * s + 1], yz[4 * s + 2], yz[4 * s + 3], vc);
+                    if (F32OUT) accf = __fadd_rn(accf, __double2float_rn(h));
+                    else acc = __dadd_rn(acc, h);
+                }
+                if (F32OUT) ((float *)out)[idx] = accf;
+                else ((double *)out)[idx] = acc;
+            }
         }
-        if (F32OUT) ((float *)out)[idx] = accf;
-        else ((double *)out)[idx] = acc;
     }
+}
+
+// Threads per CTA of h_rows_kernel: the multiple of 32 in [128, 256] that
+// leaves the fewest idle threads over a row of Nx columns (ties: more).
+static int h_rows_threads(int Nx) {
+    int best = 256, waste = 1 << 30;
+    for (int t = 256; t >= 128; t -= 32) {
+        const int w = (Nx + t - 1) / t * t - Nx;
+        if (w < waste) { waste = w; best = t; }
+    }
+    return best;
 }
 
 static int launch_h_rows(bool f32out, const double *segs, int n_seg, int Nx,
                          int Nz, double dx, double dz, const VolterraConsts &vc,
                          const double *y_dev, int Ny, long n_rows, void *out,
                          cudaStream_t stream) {
-    const long total = n_rows * Nz * (long)Nx;
-    if (total == 0) return DYFOX_OK;
-    long blocks = (total + 255) / 256;
-    if (blocks > 152L * 64) blocks = 152L * 64;
-    if (f32out)
-        h_rows_kernel<true><<<(int)blocks, 256, 0, stream>>>(
-            segs, n_seg, Nx, Nz, dx, dz, vc, y_dev, Ny, n_rows, out);
-    else
-        h_rows_kernel<false><<<(int)blocks, 256, 0, stream>>>(
-            segs, n_seg, Nx, Nz, dx, dz, vc, y_dev, Ny, n_rows, out);
+    const long pairs = n_rows * (long)Nz;
+    if (pairs == 0 || Nx == 0) return DYFOX_OK;
+    // Shared memory: the column coordinates and a tile of segments, within
+    // 48 KB where the columns leave room for 64 segments, else up to 200 KB.
+    const size_t per_seg = 4 * sizeof(double), cols = (size_t)Nx * sizeof(double);
+    const size_t budget = cols + 64 * per_seg <= 48 * 1024 ? 48 * 1024
+                                                           : 200 * 1024;
+    if (cols + per_seg > budget) {
+        set_error("H rows of %d columns need more shared memory than 200 KB",
+                  Nx);
+        return DYFOX_ESMEM;
+    }
+    const long fit = (long)((budget - cols) / per_seg);
+    const int tile = n_seg < 1 ? 1 : (n_seg < fit ? n_seg : (int)fit);
+    const size_t smem = cols + (size_t)tile * per_seg;
+    const int threads = h_rows_threads(Nx);
+    const long blocks = pairs < 152L * 16 ? pairs : 152L * 16;
+    cudaError_t e = cudaSuccess;
+    if (f32out) {
+        if (smem > 48 * 1024)
+            e = cudaFuncSetAttribute(h_rows_kernel<true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+        if (!e)
+            h_rows_kernel<true><<<(int)blocks, threads, smem, stream>>>(
+                segs, n_seg, tile, Nx, Nz, dx, dz, vc, y_dev, Ny, n_rows, out);
+    } else {
+        if (smem > 48 * 1024)
+            e = cudaFuncSetAttribute(h_rows_kernel<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+        if (!e)
+            h_rows_kernel<false><<<(int)blocks, threads, smem, stream>>>(
+                segs, n_seg, tile, Nx, Nz, dx, dz, vc, y_dev, Ny, n_rows, out);
+    }
+    if (e) return cuda_status(e, "h_rows_kernel shared memory");
     count_launch(1);
     return cuda_status(cudaGetLastError(), "h_rows_kernel");
 }

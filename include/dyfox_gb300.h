@@ -85,7 +85,8 @@ int dyfox_segment_table(const double *segs, int n_seg, const double g[3],
  * summed in table order from zero; FP64 keeps each term in double, FP32
  * rounds each segment's double value to float before a float sum, as the
  * reference does (dislocations.py:166).  out: device, Ny*Nz*Nx doubles
- * (precision FP64) or floats (FP32). */
+ * (precision FP64) or floats (FP32).  DYFOX_ESMEM for rows of more than
+ * about 25,000 columns (a row's coordinates are kept in shared memory). */
 int dyfox_h_grid(const double *seg_table, int n_seg, int Nx, int Ny, int Nz,
                  double dx, double dz, double nu, double a_core,
                  int precision, void *out, void *stream);

@@ -115,8 +115,11 @@ def test_double_log_atan2_reciprocal_of_the_fp64_field(gpu):
     the ranges the field meets (offsets from a line of 1e-12 to 1e-2 m,
     any quadrant, axes and signed zeros; r^2 from 1e-24 to 1 m^2):
     atan2 within 4 ulp of the result (both are about an ulp from the exact
-    value), log within 2e-16 relative or 4e-16 absolute, the reciprocal
-    within 1 ulp."""
+    value), log within 3 ulp or 2e-16 absolute, the reciprocal within 1
+    ulp.  (log_d itself, emulated exactly on the host, is within 1.2 ulp
+    of ln x where |ln x| >= 1 and within 5e-17 absolute elsewhere: just
+    below x = 1 the table term ln(1 + j/128) - ln 2 cancels; CUDA's log is
+    within 1 ulp.)"""
     torch = gpu
     rng = np.random.default_rng(8)
     n = 1 << 20
@@ -132,7 +135,7 @@ def test_double_log_atan2_reciprocal_of_the_fp64_field(gpu):
     r2[:4] = [1.0, 2.0, 0.5, 0.7071067811865476]
     lm = _probe64(torch, 2, r2)
     lw = _probe64(torch, 3, r2)
-    assert np.all(np.abs(lm - lw) <= np.maximum(2e-16 * np.abs(lw), 4e-16))
+    assert np.all(np.abs(lm - lw) <= 3 * np.spacing(np.abs(lw)) + 2e-16)
     rm = _probe64(torch, 4, r2)
     rw = _probe64(torch, 5, r2)
     assert np.all(np.abs(rm - rw) <= np.spacing(np.abs(rw)))

@@ -309,3 +309,46 @@ def test_learned_guess_lowers_the_initial_residual(gpu):
     _, info, _ = Lm.solve_instance(w, x0=x0, tol=1e-8)
     info = np_(info) if hasattr(info, "cpu") else info
     assert info[:, 0].max() < 1e-8 and np.all(info[:, 2] == 0)
+
+
+def test_a_guess_pays_only_at_percent_level_accuracy(gpu):
+    """How accurate a starting vector must be to save GMRES work.  On one
+    instance (t 10-14 um, 16 planes, 8 deviation parameters), the solve
+    from the exact answer perturbed by smooth relative noise eps (harmonics
+    1-8 across the width, the kind of error a network makes) needs at most
+    0.85 of the zero start's inner iterations at eps = 1e-2 and at most
+    0.65 at eps = 1e-4, while eps = 0.5 (the accuracy the trained network
+    reaches: r0 0.43-0.47) saves at most a few iterations.  Over 15-60 um
+    the same measurement gave 0.64-0.82 at 1e-2 and 0.45-0.67 at 1e-4."""
+    from dyfox_gb300 import learned as Lm
+    from dyfox_gb300.workloads import learned_guess_instances
+    torch = gpu
+    rng = np.random.default_rng(5)
+    w = learned_guess_instances(1, seed=103, t_range=(10e-6, 14e-6),
+                                n_planes=16, field=64, n_s=8)[0]
+    v, info, _ = Lm.solve_instance(w, tol=1e-8)
+    its0 = float(np_(info)[:, 1].mean())
+    h0 = Lm.instance_h(w)[:, 0, :]
+    xs = (v * torch.exp(1j * h0)[None]).contiguous()
+    Nx = w["cfg"].Nx
+    xg = np.arange(Nx)
+    noise = np.zeros((len(w["s"]), len(w["ys"]), Nx), complex)
+    for k in range(1, 9):
+        a = rng.normal(size=noise.shape[:2]) + \
+            1j * rng.normal(size=noise.shape[:2])
+        ph = rng.uniform(0, 2 * np.pi, size=noise.shape[:2])
+        noise += (a[..., None] / k) * np.exp(
+            1j * (2 * np.pi * k * xg[None, None] / Nx + ph[..., None]))
+    nt = torch.from_numpy(noise).cuda()
+    nt = nt * (torch.linalg.vector_norm(xs, dim=-1, keepdim=True) /
+               torch.linalg.vector_norm(nt, dim=-1, keepdim=True))
+    its = {}
+    for eps in (0.5, 1e-2, 1e-4):
+        _, inf, _ = Lm.solve_instance(w, x0=(xs + eps * nt).contiguous(),
+                                      tol=1e-8)
+        inf = np_(inf)
+        assert inf[:, 0].max() < 1e-8 and np.all(inf[:, 2] == 0)
+        its[eps] = float(inf[:, 1].mean())
+    assert its[1e-2] <= 0.85 * its0, (its, its0)
+    assert its[1e-4] <= 0.65 * its0, (its, its0)
+    assert its[0.5] >= 0.7 * its0, (its, its0)
