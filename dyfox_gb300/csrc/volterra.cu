@@ -9,52 +9,77 @@
 namespace dyfox {
 
 // H of n_rows planes of constant y.  y_dev != NULL gives the planes' y;
-// otherwise plane r is grid row r at y = (r - Ny/2) dx.  A CTA takes one
-// (plane, depth) pair at a time, its threads the columns: the pair's
-// offsets from every segment core (Y - cy, Z - cz) and their products with
-// the line direction are formed once per pair in shared memory, the column
-// coordinates once per CTA, so that a voxel's double work is the
-// column-dependent part of the field (each value rounded as the
-// reference's per-voxel evaluation rounds it).  Segments are taken in
-// tiles of `tile`; between tiles a thread keeps its columns' partial sums
-// in `out` (the same values and order as one pass).
-template <bool F32OUT>
+// otherwise plane r is grid row r at y = (r - Ny/2) dx.  A CTA takes
+// kHPairs consecutive (plane, depth) pairs at a time, its threads their
+// columns: the pairs' offsets from every segment core (Y - cy, Z - cz) and
+// their products with the line direction are formed once per pair in
+// shared memory, the column coordinates once per CTA, so that a voxel's
+// double work is the column-dependent part of the field (each value
+// rounded as the reference's per-voxel evaluation rounds it).  Segments
+// are taken in tiles of `tile`; between tiles a thread keeps its voxels'
+// partial sums in `out` (the same values and order as one pass).  XTAB
+// (all segments in one tile, few enough to fit): the column terms
+// X = X0 - cx and X xi0 of every segment are formed once per CTA too.
+constexpr int kHPairs = 4;
+
+template <bool F32OUT, bool XTAB>
 __global__ void h_rows_kernel(const double *__restrict__ segs, int n_seg,
                               int tile, int Nx, int Nz, double dx, double dz,
                               VolterraConsts vc,
                               const double *__restrict__ y_dev, int Ny,
                               long n_rows, void *out) {
     extern __shared__ __align__(16) double hsm[];
-    double *x0 = hsm;                  // Nx: X0 of each column
-    double *yz = hsm + Nx;             // tile x 4: Y, Z, Y xi1, Z xi2
+    // Nx: X0 of each column; XTAB: n_seg x 2 x Nx: X0 - cx, (X0 - cx) xi0
+    double *x0 = hsm;
+    const size_t ncol = XTAB ? (size_t)2 * n_seg * Nx : (size_t)Nx;
+    double *yz = hsm + ncol;           // kHPairs x tile x 4: Y, Z, Y xi1, Z xi2
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (int x = tid; x < Nx; x += nt)
-        x0[x] = __dmul_rn((double)x - 0.5 * Nx, dx);
+    if (XTAB) {
+        for (int i = tid; i < n_seg * Nx; i += nt) {
+            const int s = i / Nx, x = i - s * Nx;
+            const double *sg = segs + (size_t)s * DYFOX_SEG_STRIDE;
+            const double X = __dsub_rn(__dmul_rn((double)x - 0.5 * Nx, dx),
+                                       __ldg(sg + SEG_CX));
+            x0[(size_t)2 * s * Nx + x] = X;
+            x0[(size_t)(2 * s + 1) * Nx + x] = __dmul_rn(X, __ldg(sg + SEG_XI));
+        }
+    } else {
+        for (int x = tid; x < Nx; x += nt)
+            x0[x] = __dmul_rn((double)x - 0.5 * Nx, dx);
+    }
     const long pairs = n_rows * (long)Nz;
-    for (long rk = blockIdx.x; rk < pairs; rk += gridDim.x) {
-        const long r = rk / Nz;
-        const int k = (int)(rk - r * Nz);
-        const double yv =
-            y_dev ? y_dev[r] : __dmul_rn((double)r - 0.5 * Ny, dx);
-        const double zv = __dmul_rn((double)k, dz);
+    const long groups = (pairs + kHPairs - 1) / kHPairs;
+    for (long gi = blockIdx.x; gi < groups; gi += gridDim.x) {
+        const long rk0 = gi * kHPairs;
+        const int np = pairs - rk0 < kHPairs ? (int)(pairs - rk0) : kHPairs;
         // (one pass with no segment writes zeros)
         for (int s0 = 0; s0 < n_seg || s0 == 0; s0 += tile) {
             const int ns = n_seg - s0 < tile ? n_seg - s0 : tile;
             const double *sg0 = segs + (size_t)s0 * DYFOX_SEG_STRIDE;
             __syncthreads();           // the previous tile's readers
-            for (int s = tid; s < ns; s += nt) {
+            for (int it = tid; it < np * ns; it += nt) {
+                const int pp = it / ns, s = it - pp * ns;
+                const long rk = rk0 + pp;
+                const long r = rk / Nz;
+                const int k = (int)(rk - r * Nz);
+                const double yv =
+                    y_dev ? y_dev[r] : __dmul_rn((double)r - 0.5 * Ny, dx);
+                const double zv = __dmul_rn((double)k, dz);
                 const double *sg = sg0 + (size_t)s * DYFOX_SEG_STRIDE;
                 const double Y = __dsub_rn(yv, __ldg(sg + SEG_CY));
                 const double Z = __dsub_rn(zv, __ldg(sg + SEG_CZ));
-                yz[4 * s] = Y;
-                yz[4 * s + 1] = Z;
-                yz[4 * s + 2] = __dmul_rn(Y, __ldg(sg + SEG_XI + 1));
-                yz[4 * s + 3] = __dmul_rn(Z, __ldg(sg + SEG_XI + 2));
+                double *q = yz + ((size_t)pp * tile + s) * 4;
+                q[0] = Y;
+                q[1] = Z;
+                q[2] = __dmul_rn(Y, __ldg(sg + SEG_XI + 1));
+                q[3] = __dmul_rn(Z, __ldg(sg + SEG_XI + 2));
             }
             __syncthreads();
-            for (int x = tid; x < Nx; x += nt) {
-                const double X0 = x0[x];
-                const size_t idx = (size_t)rk * Nx + x;
+            for (int it = tid; it < np * Nx; it += nt) {
+                const int pp = it / Nx, x = it - pp * Nx;
+                const double X0 = XTAB ? 0.0 : x0[x];
+                const size_t idx = (size_t)(rk0 + pp) * Nx + x;
+                const double *q = yz + (size_t)pp * tile * 4;
                 double acc = 0.0;
                 float accf = 0.0f;
                 if (s0) {
@@ -63,9 +88,17 @@ __global__ void h_rows_kernel(const double *__restrict__ segs, int n_seg,
                 }
                 for (int s = 0; s < ns; ++s) {
                     const double *sg = sg0 + (size_t)s * DYFOX_SEG_STRIDE;
+                    double X, Xx0;
+                    if (XTAB) {
+                        X = x0[(size_t)2 * s * Nx + x];
+                        Xx0 = x0[(size_t)(2 * s + 1) * Nx + x];
+                    } else {
+                        X = __dsub_rn(X0, __ldg(sg + SEG_CX));
+                        Xx0 = __dmul_rn(X, __ldg(sg + SEG_XI));
+                    }
                     const double h = h_seg_f64h(
-                        sg, __dsub_rn(X0, __ldg(sg + SEG_CX)), yz[4 * s],
-                        yz[4 * s + 1], yz[4 * s + 2], yz[4 * s + 3], vc);
+                        sg, X, q[4 * s], q[4 * s + 1], Xx0, q[4 * s + 2],
+                        q[4 * s + 3], vc);
                     if (F32OUT) accf = __fadd_rn(accf, __double2float_rn(h));
                     else acc = __dadd_rn(acc, h);
                 }
@@ -93,9 +126,11 @@ static int launch_h_rows(bool f32out, const double *segs, int n_seg, int Nx,
                          cudaStream_t stream) {
     const long pairs = n_rows * (long)Nz;
     if (pairs == 0 || Nx == 0) return DYFOX_OK;
-    // Shared memory: the column coordinates and a tile of segments, within
-    // 48 KB where the columns leave room for 64 segments, else up to 200 KB.
-    const size_t per_seg = 4 * sizeof(double), cols = (size_t)Nx * sizeof(double);
+    // Shared memory: the column coordinates and a tile of segments for
+    // kHPairs pairs, within 48 KB where the columns leave room for 64
+    // segments, else up to 200 KB.
+    const size_t per_seg = 4 * kHPairs * sizeof(double),
+                 cols = (size_t)Nx * sizeof(double);
     const size_t budget = cols + 64 * per_seg <= 48 * 1024 ? 48 * 1024
                                                            : 200 * 1024;
     if (cols + per_seg > budget) {
@@ -105,27 +140,30 @@ static int launch_h_rows(bool f32out, const double *segs, int n_seg, int Nx,
     }
     const long fit = (long)((budget - cols) / per_seg);
     const int tile = n_seg < 1 ? 1 : (n_seg < fit ? n_seg : (int)fit);
-    const size_t smem = cols + (size_t)tile * per_seg;
+    // Column tables per segment where they fit in 40 KB with the tile (a
+    // few segments: several CTAs per SM still fit).
+    const size_t xtab = (size_t)2 * n_seg * cols + (size_t)n_seg * per_seg;
+    const bool use_xtab = n_seg >= 1 && tile == n_seg && xtab <= 40 * 1024;
+    const size_t smem = use_xtab ? xtab : cols + (size_t)tile * per_seg;
     const int threads = h_rows_threads(Nx);
-    const long blocks = pairs < 152L * 16 ? pairs : 152L * 16;
-    cudaError_t e = cudaSuccess;
-    if (f32out) {
+    const long groups = (pairs + kHPairs - 1) / kHPairs;
+    const long blocks = groups < 152L * 16 ? groups : 152L * 16;
+    auto go = [&](auto kernel) {
+        cudaError_t err = cudaSuccess;
         if (smem > 48 * 1024)
-            e = cudaFuncSetAttribute(h_rows_kernel<true>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem);
-        if (!e)
-            h_rows_kernel<true><<<(int)blocks, threads, smem, stream>>>(
+            err = cudaFuncSetAttribute(
+                kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                (int)smem);
+        if (!err)
+            kernel<<<(int)blocks, threads, smem, stream>>>(
                 segs, n_seg, tile, Nx, Nz, dx, dz, vc, y_dev, Ny, n_rows, out);
-    } else {
-        if (smem > 48 * 1024)
-            e = cudaFuncSetAttribute(h_rows_kernel<false>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem);
-        if (!e)
-            h_rows_kernel<false><<<(int)blocks, threads, smem, stream>>>(
-                segs, n_seg, tile, Nx, Nz, dx, dz, vc, y_dev, Ny, n_rows, out);
-    }
+        return err;
+    };
+    const cudaError_t e =
+        f32out ? (use_xtab ? go(h_rows_kernel<true, true>)
+                           : go(h_rows_kernel<true, false>))
+               : (use_xtab ? go(h_rows_kernel<false, true>)
+                           : go(h_rows_kernel<false, false>));
     if (e) return cuda_status(e, "h_rows_kernel shared memory");
     count_launch(1);
     return cuda_status(cudaGetLastError(), "h_rows_kernel");

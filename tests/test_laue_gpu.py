@@ -77,11 +77,29 @@ def test_h_rows_match_h_plane_golden(gpu, diamond400, name):
     assert np.abs(H - want).max() <= 1e-13 * max(np.abs(want).max(), 1.0)
 
 
-def test_h_grid_matches_the_oracle(gpu, diamond400, small_grid, rng):
+def test_h_rows_over_several_segment_tiles(gpu, diamond400, small_grid,
+                                           rng):
+    """400 segments on two planes: more than one shared-memory tile of
+    segments, the partial sums carried in the output between tiles."""
+    from dyfox_gb300.dislocations import H_rows
+    geo = geo_of(small_grid)
+    segs = random_segments(diamond400, small_grid, 400, rng)
+    y = O.grid_y(geo["Ny"], geo["dx"])[[10, 50]]
+    want = O.h_rows(segs, diamond400.g_vec, diamond400.nu, diamond400.a_core,
+                    geo["Nx"], geo["Nz"], geo["dx"], geo["dz"], y)
+    got = np_(H_rows(segs, geo["Nx"], geo["Nz"], geo["dx"], geo["dz"],
+                     diamond400.g_vec, diamond400.nu, diamond400.a_core, y))
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+
+
+@pytest.mark.parametrize("n_seg", [7, 60])
+def test_h_grid_matches_the_oracle(gpu, diamond400, small_grid, rng, n_seg):
+    """7 segments: the kernel keeps every segment's column terms in shared
+    memory; 60: too many for that, the column terms per voxel."""
     from dyfox_gb300.backend import FP32, FP64
     from dyfox_gb300.dislocations import compute_H_grid
     geo = geo_of(small_grid)
-    segs = random_segments(diamond400, small_grid, 7, rng)
+    segs = random_segments(diamond400, small_grid, n_seg, rng)
     want = O.h_rows(segs, diamond400.g_vec, diamond400.nu, diamond400.a_core,
                     geo["Nx"], geo["Nz"], geo["dx"], geo["dz"],
                     O.grid_y(geo["Ny"], geo["dx"]))
