@@ -37,13 +37,16 @@ namespace dyfox {
 // Couplings of every plane: cb = ds (sigma_hbar e^{+iH}), ch = ds (sigma_h
 // e^{-iH}) with H the Volterra phase at (x_i, y_p, z_k) summed in segment
 // order; e0h = e^{-iH} at k = 0.  One thread per voxel.
-// cb32, ch32 (may be NULL): the same couplings rounded to float; cbl32,
-// chl32: the remainders, rounded to float (float-float couplings).
+// cb32, ch32 (may be NULL): the couplings of the mixed form's depth-scaled
+// march, e0^-k cb and e0^k ch with e0^k = exp(k s0 ds) formed in double,
+// rounded to float; cbl32, chl32: the remainders, rounded to float
+// (float-float couplings).
 __global__ void bragg_couple_kernel(const double *__restrict__ segs,
                                     int n_seg, int Nx, int Nz, double dx,
                                     double dz, VolterraConsts vc,
                                     const double *__restrict__ y, int n_y,
-                                    double ds, double shr, double shi,
+                                    double ds, double s0r, double s0i,
+                                    double shr, double shi,
                                     double sbr, double sbi, double2 *cb,
                                     double2 *ch, double2 *e0h, float2 *cb32,
                                     float2 *ch32, float2 *cbl32,
@@ -74,14 +77,23 @@ __global__ void bragg_couple_kernel(const double *__restrict__ segs,
         cb[idx] = vb;
         ch[idx] = vh;
         if (cb32) {
-            const float2 b32 = make_float2((float)vb.x, (float)vb.y);
-            const float2 h32 = make_float2((float)vh.x, (float)vh.y);
+            // e0^k = m (cos q, sin q); e0^-k = (cos q, -sin q) / m
+            const double m = exp(k * s0r * ds);
+            double sq, cq;
+            sincos(k * s0i * ds, &sq, &cq);
+            const double im = 1.0 / m;
+            const double2 fb = make_double2(im * (vb.x * cq + vb.y * sq),
+                                            im * (vb.y * cq - vb.x * sq));
+            const double2 fh = make_double2(m * (vh.x * cq - vh.y * sq),
+                                            m * (vh.y * cq + vh.x * sq));
+            const float2 b32 = make_float2((float)fb.x, (float)fb.y);
+            const float2 h32 = make_float2((float)fh.x, (float)fh.y);
             cb32[idx] = b32;
             ch32[idx] = h32;
-            cbl32[idx] = make_float2((float)(vb.x - (double)b32.x),
-                                     (float)(vb.y - (double)b32.y));
-            chl32[idx] = make_float2((float)(vh.x - (double)h32.x),
-                                     (float)(vh.y - (double)h32.y));
+            cbl32[idx] = make_float2((float)(fb.x - (double)b32.x),
+                                     (float)(fb.y - (double)b32.y));
+            chl32[idx] = make_float2((float)(fh.x - (double)h32.x),
+                                     (float)(fh.y - (double)h32.y));
         }
         if (k == 0) e0h[(size_t)p * Nx + x] = make_double2(c, -sn);
     }
@@ -301,7 +313,8 @@ static int bragg_prepare(const dyfox_bragg_desc *d, const BraggPlan &p,
     if (blocks > 152L * 64) blocks = 152L * 64;
     bragg_couple_kernel<<<(int)blocks, 256, 0, stream>>>(
         seg_table, d->n_seg, d->Nx, d->Nz, d->dx, d->dz,
-        volterra_consts(d->nu, d->a_core), y, d->n_y, d->ds, a->shr, a->shi,
+        volterra_consts(d->nu, d->a_core), y, d->n_y, d->ds, a->s0r, a->s0i,
+        a->shr, a->shi,
         a->sbr, a->sbi, (double2 *)a->cb, (double2 *)a->ch, (double2 *)a->e0h,
         (float2 *)a->cb32, (float2 *)a->ch32, (float2 *)a->cbl32,
         (float2 *)a->chl32);

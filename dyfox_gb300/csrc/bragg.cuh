@@ -157,15 +157,20 @@ __device__ void bragg_march(const double2 *__restrict__ cb,
     __syncthreads();
 }
 
-// The same march in single precision, for the inner (Arnoldi) products of
-// the mixed-precision solve: couplings cb, ch and the step factors in float,
-// the inputs rounded to float (NULL means zero), the result widened into
-// out.  ex0, ex1: two float2 exchange rows of Nx each (2 Nx float2); step k
-// writes the half k % 2, so one barrier a step suffices.
+// The march in single precision, for the inner (Arnoldi) products of the
+// mixed-precision solve, in the depth-scaled form A_k = e0^-k D0_k:
+//   A'(x+1) = A(x) + cb'_k(x) Dg(x),  Dg'(x-1) = (Dg(x) - ch'_k(x) A(x)) ieg
+// with cb'_k = e0^-k cb_k and ch'_k = e0^k ch_k folded into the couplings
+// (e0 does not depend on the deviation parameter), so a column-step costs
+// two complex products and one multiplication by ieg; Dg, and so the
+// result Dg(t), are unchanged.  Couplings and ieg in float, the inputs
+// rounded to float (NULL means zero), the result widened into out.  ex0,
+// ex1: two float2 exchange rows of Nx each (2 Nx float2); step k writes the
+// half k % 2, so one barrier a step suffices.
 template <int CPL>
 __device__ void bragg_march32(const float2 *__restrict__ cb,
-                              const float2 *__restrict__ ch, float2 e0,
-                              float2 ieg, int Nz, int Nx,
+                              const float2 *__restrict__ ch, float2 ieg,
+                              int Nz, int Nx,
                               const double2 *d0_in, const double2 *dg_in,
                               float2 *ex0, float2 *ex1, double2 *out) {
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -229,7 +234,7 @@ __device__ void bragg_march32(const float2 *__restrict__ cb,
                 const float2 b = cbv[i], h = chv[i];
                 const float2 u = cadd(D0[i], cmulz(b, Dg[i]));
                 const float2 v = cmulz(csub(Dg[i], cmulz(h, D0[i])), ieg);
-                e0r[x + 1 == Nx ? 0 : x + 1] = cmulz(e0, u);
+                e0r[x + 1 == Nx ? 0 : x + 1] = u;
                 e1r[x == 0 ? Nx - 1 : x - 1] = v;
             }
         }
@@ -306,63 +311,104 @@ __device__ __forceinline__ float4 ffc_fma(float4 a, float4 b, float4 c) {
     return make_float4(re.x, re.y, im.x, im.y);
 }
 
-// The down-march of bragg_march in float-float: couplings as hi (cb, ch)
-// and lo (cbl, chl) float2 planes, step factors e0, ieg as float-float,
-// inputs (NULL: zero) and the result in double.  ex0, ex1: float4 exchange
-// rows of Nx.
+// a1 b1 + a2 b2, real float-float (ff_dot2 with no addend: one two-sum).
+__device__ __forceinline__ float2 ff_dot2z(float2 a1, float2 b1, float2 a2,
+                                           float2 b2) {
+    const float p1 = __fmul_rn(a1.x, b1.x), p2 = __fmul_rn(a2.x, b2.x);
+    float e = __fadd_rn(fmaf(a1.x, b1.x, -p1), fmaf(a2.x, b2.x, -p2));
+    e = fmaf(a1.x, b1.y, e);
+    e = fmaf(a1.y, b1.x, e);
+    e = fmaf(a2.x, b2.y, e);
+    e = fmaf(a2.y, b2.x, e);
+    const float s = __fadd_rn(p1, p2);
+    const float v = __fsub_rn(s, p1);
+    e = __fadd_rn(e, __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(p2, v)));
+    const float t = __fadd_rn(s, e);
+    return make_float2(t, __fsub_rn(e, __fsub_rn(t, s)));
+}
+
+// a b, complex float-float.
+__device__ __forceinline__ float4 ffc_mul(float4 a, float4 b) {
+    const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
+    const float2 br = make_float2(b.x, b.y), bi = make_float2(b.z, b.w);
+    const float2 re = ff_dot2z(ar, br, make_float2(-a.z, -a.w), bi);
+    const float2 im = ff_dot2z(ar, bi, ai, br);
+    return make_float4(re.x, re.y, im.x, im.y);
+}
+
+// Column layout of the float-float march: column x = tid + i blockDim.x of
+// a thread, its periodic neighbours x + 1 and x - 1, and whether it exists
+// (x < Nx), formed once per march.
+template <int CPL>
+struct MarchCols {
+    int x[CPL], xp[CPL], xm[CPL];
+    bool ok[CPL];
+    __device__ __forceinline__ MarchCols(int Nx) {
+#pragma unroll
+        for (int i = 0; i < CPL; ++i) {
+            const int c = threadIdx.x + i * blockDim.x;
+            ok[i] = c < Nx;
+            x[i] = ok[i] ? c : 0;
+            xp[i] = c + 1 >= Nx ? 0 : c + 1;
+            xm[i] = c == 0 ? Nx - 1 : c - 1;
+        }
+    }
+};
+
+// The march of bragg_march32 in float-float, for the right-hand side and
+// the true residuals of the mixed-precision solve: the depth-scaled form
+// with the folded couplings as hi (cb, ch) and lo (cbl, chl) float2
+// planes, ieg as float-float, inputs (NULL: zero) and the result in
+// double.  ex0, ex1: float4 exchange rows of Nx (two barriers a step).
 template <int CPL>
 __device__ void bragg_march_ff(const float2 *__restrict__ cb,
                                const float2 *__restrict__ cbl,
                                const float2 *__restrict__ ch,
-                               const float2 *__restrict__ chl, float4 e0,
-                               float4 ieg, int Nz, int Nx,
-                               const double2 *d0_in, const double2 *dg_in,
-                               float4 *ex0, float4 *ex1, double2 *out) {
-    const int tid = threadIdx.x, nt = blockDim.x;
+                               const float2 *__restrict__ chl, float4 ieg,
+                               int Nz, int Nx, const double2 *d0_in,
+                               const double2 *dg_in, float4 *ex0,
+                               float4 *ex1, double2 *out) {
+    const MarchCols<CPL> mc(Nx);
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 D0[CPL], Dg[CPL];
+    float4 A[CPL], G[CPL];
 #pragma unroll
     for (int i = 0; i < CPL; ++i) {
-        const int x = tid + i * nt;
-        D0[i] = z4;
-        Dg[i] = z4;
-        if (x < Nx) {
-            if (d0_in) D0[i] = ffc_of(d0_in[x]);
-            if (dg_in) Dg[i] = ffc_of(dg_in[x]);
+        A[i] = z4;
+        G[i] = z4;
+        if (mc.ok[i]) {
+            if (d0_in) A[i] = ffc_of(d0_in[mc.x[i]]);
+            if (dg_in) G[i] = ffc_of(dg_in[mc.x[i]]);
         }
     }
     for (int k = 0; k < Nz - 1; ++k) {
         const size_t row = (size_t)k * Nx;
+        const float2 *cbk = cb + row, *cblk = cbl + row;
+        const float2 *chk = ch + row, *chlk = chl + row;
 #pragma unroll
         for (int i = 0; i < CPL; ++i) {
-            const int x = tid + i * nt;
-            if (x < Nx) {
-                const float2 bh = __ldg(cb + row + x), bl = __ldg(cbl + row + x);
-                const float2 hh = __ldg(ch + row + x), hl = __ldg(chl + row + x);
+            if (mc.ok[i]) {
+                const int x = mc.x[i];
+                const float2 bh = __ldg(cbk + x), bl = __ldg(cblk + x);
+                const float2 hh = __ldg(chk + x), hl = __ldg(chlk + x);
                 const float4 b = make_float4(bh.x, bl.x, bh.y, bl.y);
                 const float4 nh = make_float4(-hh.x, -hl.x, -hh.y, -hl.y);
-                const float4 u = ffc_fma(b, Dg[i], D0[i]);
-                const float4 w = ffc_fma(nh, D0[i], Dg[i]);
-                ex0[x + 1 == Nx ? 0 : x + 1] = ffc_fma(e0, u, z4);
-                ex1[x == 0 ? Nx - 1 : x - 1] = ffc_fma(w, ieg, z4);
+                ex0[mc.xp[i]] = ffc_fma(b, G[i], A[i]);
+                ex1[mc.xm[i]] = ffc_mul(ffc_fma(nh, A[i], G[i]), ieg);
             }
         }
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < CPL; ++i) {
-            const int x = tid + i * nt;
-            if (x < Nx) {
-                D0[i] = ex0[x];
-                Dg[i] = ex1[x];
+            if (mc.ok[i]) {
+                A[i] = ex0[mc.x[i]];
+                G[i] = ex1[mc.x[i]];
             }
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < CPL; ++i) {
-        const int x = tid + i * nt;
-        if (x < Nx) out[x] = ffc_to(Dg[i]);
-    }
+    for (int i = 0; i < CPL; ++i)
+        if (mc.ok[i]) out[mc.x[i]] = ffc_to(G[i]);
     __syncthreads();
 }
 
@@ -634,9 +680,10 @@ struct BraggArgs {
     const double2 *inc;           // (Nx): incident D0
     const double2 *iT;            // (n_s, Nx): 1 / T22s
     const double2 *tw;            // (Nx): exp(-2 pi i m / Nx)
-    const float2 *cb32, *ch32;    // FP32 copies of cb, ch (mixed form)
-    const float2 *cbl32, *chl32;  // cb - cb32, ch - ch32 rounded to float:
-                                  // the float-float couplings (mixed form)
+    const float2 *cb32, *ch32;    // e0^-k cb, e0^k ch rounded to float:
+                                  // the mixed form's depth-scaled march
+    const float2 *cbl32, *chl32;  // their remainders rounded to float: the
+                                  // float-float couplings (mixed form)
     const float2 *iT32, *tw32;    // FP32 copies of iT, tw (mixed form)
     FftPlan plan;
     double2 *V;                   // (n_sys, m + 1, Nx)

@@ -86,13 +86,12 @@ __device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
     double2 *B = a.B + (size_t)sys * Nx;
     double2 e0, ieg;
     step_factors(a, is, e0, ieg);
-    const float2 e0f = make_float2((float)e0.x, (float)e0.y);
     const float2 iegf = make_float2((float)ieg.x, (float)ieg.y);
     const float2 *cb32 = MIXED ? a.cb32 + (size_t)iy * a.Nz * Nx : nullptr;
     const float2 *ch32 = MIXED ? a.ch32 + (size_t)iy * a.Nz * Nx : nullptr;
     const float2 *cbl32 = MIXED ? a.cbl32 + (size_t)iy * a.Nz * Nx : nullptr;
     const float2 *chl32 = MIXED ? a.chl32 + (size_t)iy * a.Nz * Nx : nullptr;
-    const float4 e0ff = ffc_of(e0), iegff = ffc_of(ieg);
+    const float4 iegff = ffc_of(ieg);
     const float2 *iT32 = MIXED ? a.iT32 + (size_t)is * Nx : nullptr;
     const double eps = 2.220446049250313e-16;
 
@@ -105,7 +104,7 @@ __device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
     // float-float when MIXED (the right-hand side and the true residuals).
     auto matvec = [&](const double2 *src) {
         if (MIXED) {
-            bragg_march_ff<CPL>(cb32, cbl32, ch32, chl32, e0ff, iegff, a.Nz,
+            bragg_march_ff<CPL>(cb32, cbl32, ch32, chl32, iegff, a.Nz,
                                 Nx, src ? nullptr : a.inc, src,
                                 reinterpret_cast<float4 *>(A0),
                                 reinterpret_cast<float4 *>(A1), W);
@@ -120,7 +119,7 @@ __device__ __forceinline__ int gmres_system(const BraggArgs &a, int sys,
     // The Arnoldi operator: W <- M A src, in single precision when MIXED.
     auto inner_op = [&](const double2 *src) {
         if (MIXED) {
-            bragg_march32<CPL>(cb32, ch32, e0f, iegf, a.Nz, Nx, nullptr, src,
+            bragg_march32<CPL>(cb32, ch32, iegf, a.Nz, Nx, nullptr, src,
                                reinterpret_cast<float2 *>(A0),
                                reinterpret_cast<float2 *>(A1), W);
         } else {
@@ -402,7 +401,7 @@ __global__ void bragg_apply_kernel(const BraggArgs a, int mode,
                                 a.cbl32 + (size_t)iy * a.Nz * Nx,
                                 a.ch32 + (size_t)iy * a.Nz * Nx,
                                 a.chl32 + (size_t)iy * a.Nz * Nx,
-                                ffc_of(e0), ffc_of(ieg), a.Nz, Nx,
+                                ffc_of(ieg), a.Nz, Nx,
                                 d0 ? d0 + off : nullptr,
                                 dg ? dg + off : nullptr,
                                 reinterpret_cast<float4 *>(A0),
@@ -413,7 +412,6 @@ __global__ void bragg_apply_kernel(const BraggArgs a, int mode,
         if (MIXED)
             bragg_march32<CPL>(a.cb32 + (size_t)iy * a.Nz * Nx,
                                a.ch32 + (size_t)iy * a.Nz * Nx,
-                               make_float2((float)e0.x, (float)e0.y),
                                make_float2((float)ieg.x, (float)ieg.y), a.Nz,
                                Nx, d0 ? d0 + off : nullptr,
                                dg ? dg + off : nullptr,
