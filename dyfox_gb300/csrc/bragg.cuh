@@ -164,98 +164,110 @@ __device__ void bragg_march(const double2 *__restrict__ cb,
 // (e0 does not depend on the deviation parameter), so a column-step costs
 // two complex products and one multiplication by ieg; Dg, and so the
 // result Dg(t), are unchanged.  Couplings and ieg in float, the inputs
-// rounded to float (NULL means zero), the result widened into out.  ex0,
-// ex1: two float2 exchange rows of Nx each (2 Nx float2); step k writes the
-// half k % 2, so one barrier a step suffices.
+// rounded to float (NULL means zero), the result widened into out.
+//   Thread t holds the CPL contiguous columns [t CPL, (t+1) CPL) of the row
+// in registers (threads past column Nx - 1 hold padding, kept zero).  The
+// one-column shifts move in registers, across lanes by warp shuffle, and
+// across warps and around the periodic ends (column Nx - 1 to 0 and back)
+// through a few shared slots at the start of ex0, double-buffered by the
+// step's parity: one barrier a step.  ex1 is unused.
 template <int CPL>
 __device__ void bragg_march32(const float2 *__restrict__ cb,
                               const float2 *__restrict__ ch, float2 ieg,
-                              int Nz, int Nx,
-                              const double2 *d0_in, const double2 *dg_in,
-                              float2 *ex0, float2 *ex1, double2 *out) {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    float2 D0[CPL], Dg[CPL];
+                              int Nz, int Nx, const double2 *d0_in,
+                              const double2 *dg_in, float2 *ex0, float2 *ex1,
+                              double2 *out) {
+    (void)ex1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nw = blockDim.x >> 5;
+    const int x0 = tid * CPL;
+    const int last = (Nx - 1) / CPL, jl = Nx - 1 - last * CPL;
+    const bool is_last = tid == last, is_first = tid == 0;
+    // sU[p][w]: the last column's u of warp w; sV[p][w]: the first column's
+    // v of warp w; sW[p]: (u of column Nx - 1, v of column 0)
+    float2 *sU = ex0, *sV = ex0 + 2 * nw, *sW = ex0 + 4 * nw;
+    const float2 z = make_float2(0.f, 0.f);
+    bool valid[CPL];
+    float2 A[CPL], G[CPL], b[CPL], h[CPL];
+    const int ns = Nz - 1;
 #pragma unroll
-    for (int i = 0; i < CPL; ++i) {
-        const int x = tid + i * nt;
-        D0[i] = make_float2(0.f, 0.f);
-        Dg[i] = make_float2(0.f, 0.f);
-        if (x < Nx) {
+    for (int j = 0; j < CPL; ++j) {
+        const int x = x0 + j;
+        valid[j] = x < Nx;
+        A[j] = z;
+        G[j] = z;
+        b[j] = z;
+        h[j] = z;
+        if (valid[j]) {
             if (d0_in) {
                 const double2 v = d0_in[x];
-                D0[i] = make_float2((float)v.x, (float)v.y);
+                A[j] = make_float2((float)v.x, (float)v.y);
             }
             if (dg_in) {
                 const double2 v = dg_in[x];
-                Dg[i] = make_float2((float)v.x, (float)v.y);
+                G[j] = make_float2((float)v.x, (float)v.y);
+            }
+            if (ns > 0) {
+                b[j] = __ldg(cb + x);
+                h[j] = __ldg(ch + x);
             }
         }
     }
-    // Up to 8 columns a thread, the couplings of step k + 1 are loaded while
-    // step k is computed (the march waits on these loads more than on its
-    // arithmetic: 3% on config 1); with 16 the extra registers would spill.
-    constexpr bool kPre = CPL <= 8;
-    float2 nb[CPL], nh[CPL];
+    for (int k = 0; k < ns; ++k) {
+        const int p = k & 1;
+        float2 u[CPL], v[CPL];
 #pragma unroll
-    for (int i = 0; i < CPL; ++i) {
-        const int x = tid + i * nt;
-        if (kPre && x < Nx && Nz > 1) {
-            nb[i] = __ldg(cb + x);
-            nh[i] = __ldg(ch + x);
+        for (int j = 0; j < CPL; ++j) {
+            u[j] = cadd(A[j], cmulz(b[j], G[j]));
+            v[j] = cmulz(csub(G[j], cmulz(h[j], A[j])), ieg);
         }
-    }
-    for (int k = 0; k < Nz - 1; ++k) {
-        float2 *e0r = ex0 + (k & 1) * Nx, *e1r = ex1 + (k & 1) * Nx;
-        float2 cbv[CPL], chv[CPL];
+        // the couplings of step k + 1
+        if (k + 1 < ns) {
+            const float2 *cbn = cb + (size_t)(k + 1) * Nx + x0;
+            const float2 *chn = ch + (size_t)(k + 1) * Nx + x0;
 #pragma unroll
-        for (int i = 0; i < CPL; ++i) {
-            const int x = tid + i * nt;
-            if (kPre) {
-                cbv[i] = nb[i];
-                chv[i] = nh[i];
-            } else if (x < Nx) {
-                cbv[i] = __ldg(cb + (size_t)k * Nx + x);
-                chv[i] = __ldg(ch + (size_t)k * Nx + x);
+            for (int j = 0; j < CPL; ++j) {
+                if (valid[j]) {
+                    b[j] = __ldg(cbn + j);
+                    h[j] = __ldg(chn + j);
+                }
             }
         }
-        if (kPre && k + 2 < Nz) {
-            const float2 *cbn = cb + (size_t)(k + 1) * Nx;
-            const float2 *chn = ch + (size_t)(k + 1) * Nx;
+        float2 uin, vin;
+        uin.x = __shfl_up_sync(0xffffffffu, u[CPL - 1].x, 1);
+        uin.y = __shfl_up_sync(0xffffffffu, u[CPL - 1].y, 1);
+        vin.x = __shfl_down_sync(0xffffffffu, v[0].x, 1);
+        vin.y = __shfl_down_sync(0xffffffffu, v[0].y, 1);
+        if (lane == 31) sU[p * nw + warp] = u[CPL - 1];
+        if (lane == 0) sV[p * nw + warp] = v[0];
+        if (is_last) {
+            float2 ul = u[0];
 #pragma unroll
-            for (int i = 0; i < CPL; ++i) {
-                const int x = tid + i * nt;
-                if (x < Nx) { nb[i] = __ldg(cbn + x); nh[i] = __ldg(chn + x); }
-            }
+            for (int j = 1; j < CPL; ++j)
+                if (j == jl) ul = u[j];
+            sW[2 * p] = ul;
         }
-#pragma unroll
-        for (int i = 0; i < CPL; ++i) {
-            const int x = tid + i * nt;
-            if (x < Nx) {
-                const float2 b = cbv[i], h = chv[i];
-                const float2 u = cadd(D0[i], cmulz(b, Dg[i]));
-                const float2 v = cmulz(csub(Dg[i], cmulz(h, D0[i])), ieg);
-                e0r[x + 1 == Nx ? 0 : x + 1] = u;
-                e1r[x == 0 ? Nx - 1 : x - 1] = v;
-            }
-        }
-        // The rows of step k are complete; those of step k - 1 (the other
-        // half) were read by every thread before it wrote step k.
+        if (is_first) sW[2 * p + 1] = v[0];
         __syncthreads();
+        if (lane == 0) uin = is_first ? sW[2 * p] : sU[p * nw + warp - 1];
+        if (lane == 31 && tid < last) vin = sV[p * nw + warp + 1];
 #pragma unroll
-        for (int i = 0; i < CPL; ++i) {
-            const int x = tid + i * nt;
-            if (x < Nx) {
-                D0[i] = e0r[x];
-                Dg[i] = e1r[x];
-            }
+        for (int j = CPL - 1; j >= 1; --j) A[j] = valid[j] ? u[j - 1] : z;
+        A[0] = valid[0] ? uin : z;
+#pragma unroll
+        for (int j = 0; j + 1 < CPL; ++j) G[j] = valid[j] ? v[j + 1] : z;
+        G[CPL - 1] = valid[CPL - 1] ? vin : z;
+        if (is_last) {
+            const float2 w = sW[2 * p + 1];
+#pragma unroll
+            for (int j = 0; j < CPL; ++j)
+                if (j == jl) G[j] = w;
         }
     }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < CPL; ++i) {
-        const int x = tid + i * nt;
-        if (x < Nx) out[x] = make_double2(Dg[i].x, Dg[i].y);
-    }
+    for (int j = 0; j < CPL; ++j)
+        if (valid[j]) out[x0 + j] = make_double2(G[j].x, G[j].y);
     __syncthreads();
 }
 
