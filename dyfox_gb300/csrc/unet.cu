@@ -860,7 +860,18 @@ static int unet_backward_impl(dyfox_unet *u, const float *target, float *loss,
         a.part = u->wpart;
         a.N = n; a.H = h; a.W = w; a.Cin = ci; a.Cout = co;
         a.M = 9 * ci; a.Ncols = co; a.K = (int)Pi;
-        {
+        TcWgrad tw;
+        tw.X = a.X; tw.G = a.G; tw.part = u->wpart;
+        tw.part_floats = u->wpart_floats;
+        tw.N = n; tw.H = h; tw.W = w; tw.Cin = ci; tw.Cout = co;
+        int tsplits = 0;
+        if (conv_tc_wgrad_supported(tw) &&
+            conv_tc_wgrad_launch(tw, &tsplits, s) == cudaSuccess) {
+            wgrad_reduce_kernel<<<grid_for((long)conv_wsize(i)), 256, 0, s>>>(
+                u->wpart, u->grads + u->off_w[i], tsplits, ci, co);
+            count_launch(1);
+            if ((e = cudaGetLastError())) return cuda_status(e, "unet wgrad");
+        } else {
             // splits are bounded by the partial buffer
             ConvArgs b = a;
             const int BN = co >= 64 && co % 64 == 0 ? 64 : 32;
@@ -1134,6 +1145,23 @@ extern "C" int dyfox_unet_conv(int mode, const void *X, const void *G,
         if (!X || !G || !out) {
             set_error("NULL argument");
             return DYFOX_EINVAL;
+        }
+        if (!legacy && workspace) {
+            TcWgrad tw;
+            tw.X = X; tw.G = G; tw.part = (float *)workspace;
+            tw.part_floats = workspace_bytes / sizeof(float);
+            tw.N = N; tw.H = H; tw.W = W; tw.Cin = Cin; tw.Cout = Cout;
+            int tsplits = 0;
+            if (tw.part_floats >= (size_t)9 * Cin * Cout &&
+                conv_tc_wgrad_supported(tw)) {
+                if ((e = conv_tc_wgrad_launch(tw, &tsplits, s)))
+                    return cuda_status(e, "unet conv");
+                wgrad_reduce_kernel<<<grid_for((long)9 * Cin * Cout), 256, 0,
+                                      s>>>(tw.part, (float *)out, tsplits, Cin,
+                                           Cout);
+                count_launch(1);
+                return cuda_status(cudaGetLastError(), "unet conv");
+            }
         }
         a.X = (const bf16 *)X; a.G = (const bf16 *)G;
         a.M = 9 * Cin; a.Ncols = Cout; a.K = N * H * W;

@@ -346,6 +346,186 @@ conv_tc_kernel(const __grid_constant__ CUtensorMap mapA,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient C[(t,ci)][co] = sum_p X[p + t][ci] G[p][co]: M = 9 Cin
+// rows (tap, input channel), N = Cout, K = pixels, split over pixel tiles.
+// A CTA computes 128 rows x BN channels for its share of the pixel tiles
+// into TMEM and writes the FP32 partial (split, 9 Cin, Cout) that
+// wgrad_reduce_kernel sums in split order.  Both operands are pixel-major
+// in memory, so both are MN-major for the tensor core: a K-step is one
+// tile of 128 pixels, its A operand four TMA boxes of (32 channels x 128
+// pixels) of X, each displaced by its tap (zero padding from the tensor
+// map's bounds), its B operand BN / 32 boxes of G; every box lands as 128
+// rows of 64 bytes, 64-byte swizzled (8-row atoms of 512 bytes).  In the
+// shared-memory descriptor of such an MN-major operand the leading offset
+// is the distance between 32-element atoms along M (or N), 8 KB here, and
+// the stride offset the distance between 8-row groups along K, 512 bytes;
+// an MMA of K = 16 takes two groups, so the start advances by 1 KB.
+constexpr int kTwStages = 3;
+constexpr unsigned kTwBox = kTcM * kTcK * 2;     // 8 KB: 128 pixels x 32 ch
+
+struct TwParams {
+    int H, W, Cin, Cout, BN, M9;
+    int bw, bh;
+    int ptiles, tps;        // pixel tiles in all, per split
+    float *part;
+};
+
+__host__ __device__ inline size_t tw_stage_bytes(int BN) {
+    return (size_t)4 * kTwBox + (size_t)(BN / kTcK) * kTwBox;
+}
+__host__ __device__ inline size_t tw_smem_bytes(int BN) {
+    return 1024 + kTwStages * tw_stage_bytes(BN) + 256;
+}
+
+// Descriptor of an MN-major operand: atoms of 32 elements (64 bytes) along
+// M or N `lbo` bytes apart, 8-row groups along K 512 bytes apart.
+__device__ __forceinline__ unsigned long long sw64_desc_mn(const void *p,
+                                                           unsigned lbo) {
+    const unsigned long long a = smem_u32(p);
+    return ((a & 0x3FFFFull) >> 4)
+           | ((unsigned long long)(lbo >> 4) << 16)
+           | ((512ull >> 4) << 32)
+           | (1ull << 46)
+           | (4ull << 61);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+conv_tc_wgrad_kernel(const __grid_constant__ CUtensorMap mapX,
+                     const __grid_constant__ CUtensorMap mapG,
+                     const TwParams p) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const size_t stage_bytes = tw_stage_bytes(p.BN);
+    unsigned char *ring = smem;
+    unsigned long long *full =
+        reinterpret_cast<unsigned long long *>(ring + kTwStages * stage_bytes);
+    unsigned long long *empty = full + kTwStages;
+    unsigned long long *done = empty + kTwStages;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(done + 1);
+    int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * kTcM, n0 = blockIdx.y * p.BN, z = blockIdx.z;
+    const int pt0 = z * p.tps;
+    const int npt = p.ptiles - pt0 < p.tps ? p.ptiles - pt0 : p.tps;
+    const int per_img = p.H * p.W / kTcM;
+    const int ncols_tmem = p.BN <= 32 ? 32 : p.BN <= 64 ? 64 : 128;
+    const int nb = p.BN / kTcK;
+    // A atoms of this tile inside the 9 Cin rows
+    int na = 0;
+    while (na < 4 && m0 + na * kTcK < p.M9) ++na;
+
+    if (tid == 0) {
+        for (int s = 0; s < kTwStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile(
+            "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+            ::"r"(smem_u32(tmem_slot)), "r"(ncols_tmem)
+            : "memory");
+        asm volatile(
+            "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::
+                : "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tmem_slot;
+
+    if (tid == 0) {
+        // both operands MN-major (bits 15, 16)
+        const unsigned idesc = idesc_bf16(p.BN) | (1u << 15) | (1u << 16);
+        const unsigned bytes = (unsigned)(na + nb) * kTwBox;
+        bool ok = true;
+        int issued = 0, consumed = 0;
+        for (int it = 0; it < npt + kTwStages - 1 && ok; ++it) {
+            if (it < npt) {
+                const int s = it % kTwStages;
+                if (it >= kTwStages)
+                    ok = mbar_wait(&empty[s], ((it / kTwStages) - 1) & 1,
+                                   TC_EMPTY_TIMEOUT);
+                if (!ok) break;
+                const int tile = pt0 + it;
+                const int img = tile / per_img;
+                const int q0 = (tile - img * per_img) * kTcM;
+                const int y0 = q0 / p.W, x0 = q0 - y0 * p.W;
+                unsigned char *sa = ring + s * stage_bytes;
+                unsigned char *sb = sa + 4 * kTwBox;
+                mbar_expect_tx(&full[s], bytes);
+                for (int a = 0; a < na; ++a) {
+                    const int m = m0 + a * kTcK;
+                    const int t = m / p.Cin, c0 = m - t * p.Cin;
+                    tma_load_4d(sa + a * kTwBox, &mapX, c0, x0 + t % 3 - 1,
+                                y0 + t / 3 - 1, img, &full[s]);
+                }
+                for (int b = 0; b < nb; ++b)
+                    tma_load_4d(sb + b * kTwBox, &mapG, n0 + b * kTcK, x0, y0,
+                                img, &full[s]);
+                ++issued;
+            }
+            const int j = it - (kTwStages - 1);
+            if (j >= 0) {
+                const int s = j % kTwStages;
+                ok = mbar_wait(&full[s], (j / kTwStages) & 1, TC_FULL_TIMEOUT);
+                if (!ok) break;
+                ++consumed;
+                tc_fence_after();
+                const unsigned char *sa = ring + s * stage_bytes;
+                const unsigned char *sb = sa + 4 * kTwBox;
+#pragma unroll
+                for (int kk = 0; kk < kTcM / 16; ++kk)
+                    tc_mma(tmem, sw64_desc_mn(sa + 1024 * kk, kTwBox),
+                           sw64_desc_mn(sb + 1024 * kk, kTwBox), idesc,
+                           (j > 0 || kk > 0) ? 1u : 0u);
+                tc_commit(&empty[s]);
+            }
+        }
+        if (!ok) {
+            *abort_flag = 1;
+            for (int j = consumed; j < issued; ++j)
+                mbar_wait(&full[j % kTwStages], (j / kTwStages) & 1,
+                          TC_FULL_TIMEOUT);
+        }
+        tc_commit(done);
+    }
+    __syncwarp();
+    const bool done_ok = mbar_wait(done, 0, TC_DONE_TIMEOUT);
+    tc_fence_after();
+    __syncthreads();
+    const int row = warp * 32 + lane;
+    const int m = m0 + row;
+    if (done_ok && !*abort_flag && m < p.M9) {
+        const unsigned lane_base = tmem + ((unsigned)(warp * 32) << 16);
+        float *dst = p.part + ((size_t)z * p.M9 + m) * p.Cout + n0;
+        for (int c = 0; c < p.BN; c += 16) {
+            float v[16];
+            tmem_ld16(lane_base + (unsigned)c, v);
+            float4 *d4 = reinterpret_cast<float4 *>(dst + c);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                d4[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2],
+                                    v[4 * i + 3]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile(
+            "tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+            "r"(ncols_tmem)
+            : "memory");
+    }
+}
+
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
                                  void *, const cuuint64_t *, const cuuint64_t *,
                                  const cuuint32_t *, const cuuint32_t *,
@@ -438,6 +618,69 @@ cudaError_t conv_tc_launch(const TcConv &c, cudaStream_t stream) {
     dim3 grid((unsigned)tiles, (unsigned)(c.Ncols / p.BN), 1);
     conv_tc_kernel<<<grid, kTcThreads, smem, stream>>>(mapA, mapB, p);
     count_launch(1);
+    return cudaGetLastError();
+}
+
+bool conv_tc_wgrad_supported(const TcWgrad &w) {
+    if (w.Cin % kTcK || w.Cout % kTcK) return false;
+    if (w.W >= kTcM ? w.W % kTcM != 0 : (kTcM % w.W != 0 || w.H % (kTcM / w.W)))
+        return false;
+    if (((long)w.H * w.W) % kTcM) return false;
+    if ((uintptr_t)w.X % 16 || (uintptr_t)w.G % 16 || (uintptr_t)w.part % 16)
+        return false;
+    return encode_fn() != nullptr;
+}
+
+cudaError_t conv_tc_wgrad_launch(const TcWgrad &w, int *splits,
+                                 cudaStream_t stream) {
+    EncodeTiled enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    TwParams p;
+    memset(&p, 0, sizeof p);
+    p.H = w.H; p.W = w.W; p.Cin = w.Cin; p.Cout = w.Cout;
+    p.M9 = 9 * w.Cin;
+    p.BN = w.Cout <= 128 ? w.Cout : (w.Cout % 128 == 0 ? 128 : 64);
+    if (w.Cout % p.BN) p.BN = 32;
+    p.bw = w.W >= kTcM ? kTcM : w.W;
+    p.bh = kTcM / p.bw;
+    p.part = w.part;
+    p.ptiles = (int)((long)w.N * w.H * w.W / kTcM);
+    const int mt = (p.M9 + kTcM - 1) / kTcM, nt = w.Cout / p.BN;
+    // about two CTAs per SM, bounded by the partial buffer and the tiles
+    int sp = (2 * 152 + mt * nt - 1) / (mt * nt);
+    const long cap = (long)(w.part_floats / ((size_t)p.M9 * w.Cout));
+    if (sp > cap) sp = (int)cap;
+    if (sp > p.ptiles) sp = p.ptiles;
+    if (sp < 1) return cudaErrorInvalidValue;
+    p.tps = (p.ptiles + sp - 1) / sp;
+    const int z = (p.ptiles + p.tps - 1) / p.tps;
+
+    CUtensorMap mapX, mapG;
+    auto act_map = [&](CUtensorMap *map, const void *ptr, int C) {
+        const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)w.W,
+                                    (cuuint64_t)w.H, (cuuint64_t)w.N};
+        const cuuint64_t strides[3] = {(cuuint64_t)C * 2,
+                                       (cuuint64_t)w.W * C * 2,
+                                       (cuuint64_t)w.H * w.W * C * 2};
+        const cuuint32_t box[4] = {kTcK, (cuuint32_t)p.bw, (cuuint32_t)p.bh, 1};
+        const cuuint32_t estr[4] = {1, 1, 1, 1};
+        return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+                   const_cast<void *>(ptr), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    };
+    if (!act_map(&mapX, w.X, w.Cin) || !act_map(&mapG, w.G, w.Cout))
+        return cudaErrorInvalidValue;
+    const size_t smem = tw_smem_bytes(p.BN);
+    cudaError_t e = cudaFuncSetAttribute(
+        conv_tc_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)mt, (unsigned)nt, (unsigned)z);
+    conv_tc_wgrad_kernel<<<grid, kTcThreads, smem, stream>>>(mapX, mapG, p);
+    count_launch(1);
+    *splits = z;
     return cudaGetLastError();
 }
 

@@ -1,5 +1,5 @@
-// The tensor-core (tcgen05) path of the U-Net's 3x3 convolution products,
-// defined in unet_tc.cu.
+// The tensor-core (tcgen05) path of the U-Net's 3x3 convolution products
+// (forward, data gradient, weight gradient), defined in unet_tc.cu.
 #pragma once
 #include "common.cuh"
 
@@ -24,5 +24,23 @@ struct TcConv {
 // 16-byte aligned buffers, and the driver's tensor-map encoder available.
 bool conv_tc_supported(const TcConv &c);
 cudaError_t conv_tc_launch(const TcConv &c, cudaStream_t stream);
+
+// The weight-gradient product: FP32 partials (splits, 9 Cin, Cout) of
+// sum_p X[p + t][ci] G[p][co] over shares of the pixels, for
+// wgrad_reduce_kernel.  X (N, H, W, Cin) and G (N, H, W, Cout) bf16;
+// part: part_floats floats.
+struct TcWgrad {
+    const void *X, *G;
+    float *part;
+    size_t part_floats;
+    int N, H, W, Cin, Cout;
+};
+
+// Whether the shapes fit (channels multiples of 32, the image rows as for
+// the other products, 16-byte aligned buffers, the encoder available).
+bool conv_tc_wgrad_supported(const TcWgrad &w);
+// Launches the partial products; *splits receives the partials written.
+cudaError_t conv_tc_wgrad_launch(const TcWgrad &w, int *splits,
+                                 cudaStream_t stream);
 
 }  // namespace dyfox

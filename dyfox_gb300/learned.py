@@ -260,9 +260,9 @@ def conv(mode, *, X=None, G=None, Wk=None, bias=None, Cin=None, Cout=None,
     mode "fwd" -> bf16 relu(conv(X, Wk) + bias), "dgrad" -> float data
     gradient of G (Wk transposed [Cin][9][Cout]), "wgrad" -> float weight
     gradient [Cout][9][Cin] of X and G.  Tensors NHWC on the GPU.  The
-    forward and data-gradient products run on the tcgen05 tensor cores when
-    the image rows fit its 128-pixel tiles; ``mma_sync=True`` takes the
-    mma.sync implicit GEMM instead."""
+    three products run on the tcgen05 tensor cores when the image rows fit
+    their 128-pixel tiles; ``mma_sync=True`` takes the mma.sync implicit
+    GEMM instead."""
     torch = _lib.torch_cuda()
     ref = X if X is not None else G
     N, H, W = ref.shape[:3]

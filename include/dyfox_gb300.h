@@ -392,10 +392,11 @@ int dyfox_unet_buffer(dyfox_unet *net, int which, int index, void **ptr,
  * Wk) + bias)) (Wk [Cout][9][Cin]); mode 1 out = data gradient of G
  * (float, (N, H, W, Cin); Wk the transposed weights [Cin][9][Cout]); mode
  * 2 out = weight gradient [Cout][9][Cin] (float) of X and G, with the
- * split partials in the workspace.  Channels multiples of 32.  Modes 0 and
- * 1 run on the tcgen05 tensor cores (TMEM accumulators, TMA-staged tiles)
- * when rows hold 128 pixels or divide 128; mode | DYFOX_CONV_MMA_SYNC runs
- * the mma.sync implicit GEMM instead (cross-checks). */
+ * split partials in the workspace.  Channels multiples of 32.  All three
+ * run on the tcgen05 tensor cores (TMEM accumulators, TMA-staged tiles)
+ * when rows hold 128 pixels or divide 128 (mode 2 also needs a workspace
+ * of at least 9 Cin Cout floats); mode | DYFOX_CONV_MMA_SYNC runs the
+ * mma.sync implicit GEMM instead (cross-checks). */
 #define DYFOX_CONV_MMA_SYNC 16
 int dyfox_unet_conv(int mode, const void *X, const void *G, const void *Wk,
                     const float *bias, void *out, int N, int H, int W,
