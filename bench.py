@@ -82,6 +82,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--once", choices=["fp32", "fp64", "bragg", "bragg32",
+                                       "bragg32-scan",
                                        "scan", "scan256", "image", "batch",
                                        "unet", "hgrid"],
                     help="run one solve of that form after one warm-up and "
@@ -686,12 +687,16 @@ def run_once(args):
             image_intensity(stack, pup)
             torch.cuda.synchronize()
         return
-    if args.once in ("bragg", "bragg32"):
+    if args.once in ("bragg", "bragg32", "bragg32-scan"):
+        # 4 deviation parameters x 8 planes, or (bragg32-scan) the whole
+        # config-1 scan, 21 x 64, in mixed precision
         from dyfox_gb300.bragg import solve_scan
         bx, bcfg, bseg, bs, bys, bg = bragg_workload()
-        prec = "fp32" if args.once == "bragg32" else "fp64"
+        prec = "fp64" if args.once == "bragg" else "fp32"
+        full = args.once == "bragg32-scan"
         for _ in range(2):
-            solve_scan(bseg, bs[:4], bcfg, bys[:8], bx, bg, precision=prec)
+            solve_scan(bseg, bs if full else bs[:4], bcfg,
+                       bys if full else bys[:8], bx, bg, precision=prec)
             torch.cuda.synchronize()
         return
     if args.once == "batch":
@@ -951,10 +956,12 @@ def batched_leg(args, world):
 
 def conv_leg(reps=20):
     """The U-Net's widest 3x3 convolution (e0b: batch 8 x 256 x 256, 32 ->
-    32 channels) forward, and the data gradient of d2a (batch 8 x 64 x 64,
-    128 -> 384 channels), on the tcgen05 tensor cores and with the mma.sync
-    implicit GEMM, CUDA events, L2 flushed between launches.  Flops = 2 M N
-    K; bytes = the activations read and written once and the weights."""
+    32 channels) forward and weight gradient, and the data gradient of d2a
+    (batch 8 x 64 x 64, 128 -> 384 channels), on the tcgen05 tensor cores
+    and with the mma.sync implicit GEMM, CUDA events, L2 flushed between
+    launches (the weight gradient's time includes its split reduction).
+    Flops = 2 M N K; bytes = the activations read and written once and the
+    weights."""
     import torch
     from dyfox_gb300.learned import conv, tc_error
     peak, src = bf16_peak()
@@ -963,8 +970,17 @@ def conv_leg(reps=20):
     res = {}
     for name, (N, H, W, Cin, Cout, mode) in (
             ("e0b_fwd", (8, 256, 256, 32, 32, "fwd")),
+            ("e0b_wgrad", (8, 256, 256, 32, 32, "wgrad")),
             ("d2a_dgrad", (8, 64, 64, 384, 128, "dgrad"))):
-        if mode == "fwd":
+        if mode == "wgrad":
+            X = torch.randn(N, H, W, Cin, device="cuda", generator=g).to(
+                torch.bfloat16)
+            G = torch.randn(N, H, W, Cout, device="cuda", generator=g).to(
+                torch.bfloat16)
+            kw = dict(X=X, G=G, Cin=Cin, Cout=Cout)
+            Ncols, K = Cout, N * H * W          # M = 9 Cin
+            nbytes = 2 * N * H * W * (Cin + Cout) + 4 * 9 * Cin * Cout
+        elif mode == "fwd":
             X = torch.randn(N, H, W, Cin, device="cuda", generator=g).to(
                 torch.bfloat16)
             Wk = (0.1 * torch.randn(Cout, 9, Cin, device="cuda",
@@ -982,7 +998,7 @@ def conv_leg(reps=20):
             Ncols, K = Cin, 9 * Cout
             nbytes = 2 * N * H * W * Cout + 4 * N * H * W * Cin + \
                 2 * Wk.numel()
-        flops = 2.0 * N * H * W * Ncols * K
+        flops = 2.0 * (9 * Cin if mode == "wgrad" else N * H * W) * Ncols * K
         entry = {"shape_N_H_W_Cin_Cout": [N, H, W, Cin, Cout],
                  "gflop": flops * 1e-9, "bytes": nbytes}
         for form, mma in (("tcgen05", False), ("mma_sync", True)):
