@@ -71,6 +71,10 @@ _SIGNATURES = {
     "dyfox_laue_solve": (c_int, [ctypes.POINTER(LaueDesc), c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_size_t, c_void_p]),
+    "dyfox_laue_solve_to_host": (c_int, [ctypes.POINTER(LaueDesc), c_void_p,
+                                         c_void_p, c_void_p, c_void_p,
+                                         c_void_p, c_void_p, c_size_t,
+                                         c_int, c_void_p, c_void_p]),
 }
 
 _lib = None

@@ -578,10 +578,16 @@ extern "C" size_t dyfox_laue_workspace_bytes(const dyfox_laue_desc *d) {
     return p.ws;
 }
 
-extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
-                                const void *h_grid, const double *seg_table,
-                                void *out, void *workspace,
-                                size_t workspace_bytes, void *stream_) {
+// The solve of dyfox_laue_solve and dyfox_laue_solve_to_host.  host_out
+// non-NULL: the march runs in batches of march_batch deviation parameters
+// (0: one batch) and each batch's exit waves are copied into host_out on
+// copy_stream, behind an event on `stream`, while the next batch marches.
+static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
+                           const void *h_grid, const double *seg_table,
+                           void *out, void *workspace,
+                           size_t workspace_bytes, void *stream_,
+                           void *host_out, int march_batch,
+                           cudaStream_t copy_stream) {
     set_error("");
     LauePlan p;
     int st = make_plan(d, &p);
@@ -629,6 +635,24 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     a.kpair = single ? (const float4 *)(ws + p.off_kpair) : nullptr;
 
     cudaError_t e;
+    // Angles [e0, e0 + ne) of out into host_out on copy_stream, after the
+    // work queued so far on `stream`.
+    const size_t wave_bytes = (size_t)d->Ny * d->Nx * elem;
+    auto copy_out = [&](int e0, int ne) -> int {
+        if (!host_out || ne <= 0) return DYFOX_OK;
+        cudaEvent_t ev;
+        cudaError_t ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (ce) return cuda_status(ce, "copy event");
+        ce = cudaEventRecord(ev, stream);
+        if (!ce) ce = cudaStreamWaitEvent(copy_stream, ev, 0);
+        if (!ce)
+            ce = cudaMemcpyAsync((char *)host_out + (size_t)e0 * wave_bytes,
+                                 (const char *)out + (size_t)e0 * wave_bytes,
+                                 (size_t)ne * wave_bytes,
+                                 cudaMemcpyDeviceToHost, copy_stream);
+        cudaEventDestroy(ev);
+        return ce ? cuda_status(ce, "exit-wave copy") : DYFOX_OK;
+    };
     laue_mark(0, stream);
     // Rows outside the beam are zero; kappa tables; pivots (one launch).
     {
@@ -668,7 +692,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     if (p.n_rows == 0) {
         laue_mark(2, stream);
         laue_mark(3, stream);
-        return DYFOX_OK;
+        return copy_out(0, d->n_e);
     }
     if (p.stage) {
         e = launch_cs_stage(single, (d->flags & DYFOX_FLAG_H_FP64) != 0,
@@ -706,7 +730,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
         }
         if ((e = cudaGetLastError())) return cuda_status(e, "laue_general");
         laue_mark(3, stream);
-        return DYFOX_OK;
+        return copy_out(0, d->n_e);
     }
 
     FastConfig fc;
@@ -716,11 +740,54 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
     a.WA = fc.WA;
     a.A = fc.A;
     a.ncols = 32 * fc.WA * fc.cpl;
-    a.n_groups = div_up(fc.pairs ? (d->n_e + 1) / 2 : d->n_e, fc.A);
     a.stage = fc.stage;
     a.raw_elem = fc.raw_elem;
-    e = fc.entry.launch(a, p.n_rows * a.n_groups, fc.block, fc.smem, stream);
-    if (e) return cuda_status(e, "laue_march");
+    // Angles per march launch: all of them, or (copies to the host) a
+    // multiple of the angles a CTA takes (of pairs' angles for the pair
+    // march), so that every batch but the last fills its CTAs.
+    const int unit = fc.pairs ? 2 * fc.A : fc.A;
+    int nb = d->n_e;
+    if (host_out && march_batch > 0 && march_batch < d->n_e)
+        nb = div_up(march_batch, unit) * unit;
+    for (int e0 = 0; e0 < d->n_e; e0 += nb) {
+        const int ne = d->n_e - e0 < nb ? d->n_e - e0 : nb;
+        MarchArgs ab = a;
+        ab.n_e = ne;
+        ab.kappa = a.kappa + (size_t)e0 * nsteps;
+        ab.kappa32 = a.kappa32 + (size_t)e0 * nsteps;
+        ab.scale = a.scale + e0;
+        ab.out = (char *)out + (size_t)e0 * wave_bytes;
+        if (a.kpair) ab.kpair = a.kpair + (size_t)(e0 / 2) * nsteps * 4;
+        ab.n_groups = div_up(fc.pairs ? (ne + 1) / 2 : ne, fc.A);
+        e = fc.entry.launch(ab, p.n_rows * ab.n_groups, fc.block, fc.smem,
+                            stream);
+        if (e) return cuda_status(e, "laue_march");
+        if ((st = copy_out(e0, ne))) return st;
+    }
     laue_mark(3, stream);
     return DYFOX_OK;
+}
+
+extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
+                                const void *h_grid, const double *seg_table,
+                                void *out, void *workspace,
+                                size_t workspace_bytes, void *stream) {
+    return laue_solve_impl(d, s_dev, h_grid, seg_table, out, workspace,
+                           workspace_bytes, stream, nullptr, 0, nullptr);
+}
+
+extern "C" int dyfox_laue_solve_to_host(
+    const dyfox_laue_desc *d, const double *s_dev, const void *h_grid,
+    const double *seg_table, void *out, void *host_out, void *workspace,
+    size_t workspace_bytes, int march_batch, void *stream,
+    void *copy_stream) {
+    if (!host_out) {
+        set_error("host_out must be host memory (pinned for the copies to "
+                  "overlap the march)");
+        return DYFOX_EINVAL;
+    }
+    return laue_solve_impl(d, s_dev, h_grid, seg_table, out, workspace,
+                           workspace_bytes, stream, host_out, march_batch,
+                           copy_stream ? (cudaStream_t)copy_stream
+                                       : (cudaStream_t)stream);
 }

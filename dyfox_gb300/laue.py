@@ -137,7 +137,7 @@ def _flags(prec, h_mode, compensated, general, h_sum, pairs="auto"):
 def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
            pristine, h_mode="auto", compensated=True, general=False,
            angles_per_cta=0, cols_per_lane=0, out=None, h_sum="ff",
-           tuned=True, pairs="auto"):
+           tuned=True, pairs="auto", host_out=None):
     torch = _lib.torch_cuda()
     prec = as_precision(precision)
     s = np.atleast_1d(np.asarray(s_dev_arr, dtype=float))
@@ -165,6 +165,14 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
     batch = max(1, int(batch)) if batch else n_e
     s_dev = torch.from_numpy(s).to("cuda")
     stream = _lib.stream_ptr()
+    copy_stream = None
+    if host_out is not None:
+        if (host_out.device.type != "cpu" or host_out.dtype != out.dtype or
+                tuple(host_out.shape) != tuple(out.shape) or
+                not host_out.is_contiguous()):
+            raise ValueError(f"host_out must be a contiguous CPU tensor of "
+                             f"shape {tuple(out.shape)} and dtype {out.dtype}")
+        copy_stream = torch.cuda.Stream()
     for bs in range(0, n_e, batch):
         be = min(bs + batch, n_e)
         d = _desc(xtal, geo, be - bs, prec, h_source, n_seg, ap, flags,
@@ -180,10 +188,24 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
         if nbytes == 0:
             _lib.check(_lib.DYFOX_EINVAL, "dyfox_laue_workspace_bytes")
         ws = _workspace_tensor(nbytes)
-        _lib.check(_lib.lib().dyfox_laue_solve(
-            d, _lib.c_void_p(s_dev.data_ptr() + 8 * bs), _lib.ptr(H),
-            _lib.ptr(table_dev), _lib.c_void_p(out[bs].data_ptr()),
-            _lib.ptr(ws), ws.numel(), stream), "dyfox_laue_solve")
+        if host_out is None:
+            _lib.check(_lib.lib().dyfox_laue_solve(
+                d, _lib.c_void_p(s_dev.data_ptr() + 8 * bs), _lib.ptr(H),
+                _lib.ptr(table_dev), _lib.c_void_p(out[bs].data_ptr()),
+                _lib.ptr(ws), ws.numel(), stream), "dyfox_laue_solve")
+        else:
+            # about eight march launches a call, each batch's waves copied
+            # while the next marches
+            _lib.check(_lib.lib().dyfox_laue_solve_to_host(
+                d, _lib.c_void_p(s_dev.data_ptr() + 8 * bs), _lib.ptr(H),
+                _lib.ptr(table_dev), _lib.c_void_p(out[bs].data_ptr()),
+                _lib.c_void_p(host_out[bs].data_ptr()), _lib.ptr(ws),
+                ws.numel(), max(1, (be - bs + 7) // 8), stream,
+                _lib.c_void_p(copy_stream.cuda_stream)),
+                "dyfox_laue_solve_to_host")
+    if host_out is not None:
+        copy_stream.synchronize()
+        return host_out
     return out
 
 
@@ -207,7 +229,8 @@ def describe(seg_list, s_dev_arr, grid, xtal, *, H_gpu=None,
 
 def solve_dislocation(seg_list, s_dev_arr, grid, xtal, *, H_gpu=None,
                       batch=64, precision=FP64, h_mode="auto",
-                      compensated=True, h_sum="ff", pairs="auto"):
+                      compensated=True, h_sum="ff", pairs="auto",
+                      host_out=None):
     """Exit wave of a dislocation field at each deviation parameter.
 
     ``batch`` caps the angles per launch (results do not depend on it).
@@ -218,10 +241,14 @@ def solve_dislocation(seg_list, s_dev_arr, grid, xtal, *, H_gpu=None,
     "ff", default, or in double "fp64"), ``pairs`` (FP32 compensated: march
     two deviation parameters per thread in packed f32x2 arithmetic; "auto"
     follows the autotuner and is the scalar march without a tuned shape;
-    the results are the same bits either way).
+    the results are the same bits either way), ``host_out`` (a contiguous
+    CPU tensor, pinned for speed, of the result's shape and dtype: the exit
+    waves are copied into it while the march proceeds, in about eight
+    batches of angles a call, and it is returned once complete).
     """
     return _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
-                  False, h_mode, compensated, h_sum=h_sum, pairs=pairs)
+                  False, h_mode, compensated, h_sum=h_sum, pairs=pairs,
+                  host_out=host_out)
 
 
 def solve_pristine(s_dev_arr, grid, xtal, *, precision=FP64):

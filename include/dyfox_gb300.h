@@ -139,6 +139,21 @@ int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
                      const void *h_grid, const double *seg_table, void *out,
                      void *workspace, size_t workspace_bytes, void *stream);
 
+/* dyfox_laue_solve with the exit waves also copied into host memory while
+ * the march proceeds: the march runs in batches of about march_batch
+ * deviation parameters (rounded up to whole CTAs; 0 or >= n_e: one
+ * batch), and after each batch its waves out[e0 .. e0 + nb) are copied
+ * into host_out (same layout; pinned, for the copies to overlap) on
+ * copy_stream (NULL: `stream`), behind an event on `stream`.  Returns
+ * once the work is queued; host_out is complete when copy_stream is.  No
+ * DYFOX counterpart (DYFOX returns device arrays): the copy of a
+ * 256-angle scan's 1.2 GB of waves hides behind its march. */
+int dyfox_laue_solve_to_host(const dyfox_laue_desc *d, const double *s_dev,
+                             const void *h_grid, const double *seg_table,
+                             void *out, void *host_out, void *workspace,
+                             size_t workspace_bytes, int march_batch,
+                             void *stream, void *copy_stream);
+
 /* dyfox_laue_solve for callers that cannot allocate device memory when
  * they solve (no counterpart in the DYFOX reference).  Examples: a real-time
  * acquisition or reconstruction loop that reserves its device memory once

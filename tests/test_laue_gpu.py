@@ -348,6 +348,38 @@ def test_fused_and_staged_phase_agree_bitwise(gpu, diamond400, small_grid,
     assert a.tobytes() == b.tobytes()
 
 
+@pytest.mark.parametrize("prec,h_mode,pairs", [("fp32", "staged", False),
+                                              ("fp32", "fused", False),
+                                              ("fp32", "staged", True),
+                                              ("fp64", "auto", False)])
+def test_host_out_copies_every_angle_batch(gpu, diamond400, small_grid, rng,
+                                           prec, h_mode, pairs):
+    """host_out: the march in batches of angles with each batch's waves
+    copied to pinned host memory while the next marches gives the device
+    call's bytes, for angle counts that leave a short last batch, through
+    the scalar and the pair march and in FP64; a host_out of the wrong
+    shape is refused."""
+    from dyfox_gb300.laue import _solve, solve_dislocation
+    torch = gpu
+    segs = random_segments(diamond400, small_grid, 3, rng)
+    for n_e in (2, 19, 40):
+        s = np.linspace(-3e5, 3e5, n_e)
+        kw = dict(precision=prec, h_mode=h_mode, batch=n_e)
+        want = np_(_solve(segs, s, small_grid, diamond400, None, n_e, prec,
+                          False, h_mode=h_mode, pairs=pairs, tuned=False))
+        host = torch.empty(want.shape, dtype=torch.complex64 if prec ==
+                           "fp32" else torch.complex128, pin_memory=True)
+        host.fill_(float("nan"))
+        got = _solve(segs, s, small_grid, diamond400, None, n_e, prec, False,
+                     h_mode=h_mode, pairs=pairs, tuned=False, host_out=host)
+        assert got is host
+        assert host.numpy().tobytes() == want.tobytes(), n_e
+    with pytest.raises(ValueError):
+        solve_dislocation(segs, s[:3], small_grid, diamond400,
+                          host_out=torch.empty(1, dtype=torch.complex128),
+                          **kw)
+
+
 @pytest.mark.parametrize("h_mode,h_sum", [("fused", "ff"),
                                            ("fused", "fp64"),
                                            ("staged", "ff")])
