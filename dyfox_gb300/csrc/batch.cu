@@ -106,8 +106,12 @@ laue_batch_kernel(const LaueInst *__restrict__ insts,
                               k0, kn, s_sum64 != 0, slab, smem);
             }
         }
+        // staged rows: the march specialised for them at compile time
         for (int g = 0; g < a.n_groups; ++g) {
-            march_block<float, CPL, HT_GENERIC, true>(a, 0, g, smem);
+            if (a.hsrc == HS_CS32)
+                march_block<float, CPL, HT_STAGED, true>(a, 0, g, smem);
+            else
+                march_block<float, CPL, HT_GENERIC, true>(a, 0, g, smem);
             __syncthreads();
         }
     }
