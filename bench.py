@@ -403,8 +403,8 @@ def run_ours(args):
     s_host = np.asarray(s, float)
 
     def e2e():
-        # the exit waves land in pinned host memory, copied batch by batch
-        # while the march proceeds
+        # the exit waves land in pinned host memory, copied row chunk by
+        # row chunk while the march proceeds
         solve_dislocation(segs, s_host, grid, x, precision=FP32,
                           h_mode="staged", h_sum="fp64", batch=n_e,
                           host_out=host)
@@ -471,8 +471,8 @@ def run_ours(args):
                 "call": "solve_dislocation(segs, s_dev, grid, xtal, "
                         "precision=FP32, h_mode='staged', h_sum='fp64', "
                         "batch=256, host_out=<pinned host tensor>): the "
-                        "waves copied to the host batch by batch while the "
-                        "march proceeds"},
+                        "waves copied to the host row chunk by row chunk "
+                        "while the march proceeds"},
         "roofline": {"bound": "fp32", "kernel": "laue_march_kernel",
                      "achieved": achieved, "peak": peaks["fp32"],
                      "unit": "TFLOP/s", "frac": achieved / peaks["fp32"],

@@ -579,14 +579,15 @@ extern "C" size_t dyfox_laue_workspace_bytes(const dyfox_laue_desc *d) {
 }
 
 // The solve of dyfox_laue_solve and dyfox_laue_solve_to_host.  host_out
-// non-NULL: the march runs in batches of march_batch deviation parameters
-// (0: one batch) and each batch's exit waves are copied into host_out on
-// copy_stream, behind an event on `stream`, while the next batch marches.
+// non-NULL: the active rows are marched in n_chunks row chunks (0: 8), all
+// deviation parameters in one launch per chunk, and after each chunk's
+// march its rows of every wave are copied into host_out on copy_stream,
+// behind an event on `stream`.
 static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
                            const void *h_grid, const double *seg_table,
                            void *out, void *workspace,
                            size_t workspace_bytes, void *stream_,
-                           void *host_out, int march_batch,
+                           void *host_out, int n_chunks,
                            cudaStream_t copy_stream) {
     set_error("");
     LauePlan p;
@@ -635,21 +636,28 @@ static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
     a.kpair = single ? (const float4 *)(ws + p.off_kpair) : nullptr;
 
     cudaError_t e;
-    // Angles [e0, e0 + ne) of out into host_out on copy_stream, after the
-    // work queued so far on `stream`.
-    const size_t wave_bytes = (size_t)d->Ny * d->Nx * elem;
-    auto copy_out = [&](int e0, int ne) -> int {
-        if (!host_out || ne <= 0) return DYFOX_OK;
+    // Rows [r0, r0 + nr) of every angle of out into host_out on
+    // copy_stream, after the work queued so far on `stream` (one strided
+    // copy: n_e slices of nr rows).
+    auto copy_rows = [&](int r0, int nr) -> int {
+        if (!host_out || nr <= 0) return DYFOX_OK;
         cudaEvent_t ev;
         cudaError_t ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
         if (ce) return cuda_status(ce, "copy event");
         ce = cudaEventRecord(ev, stream);
         if (!ce) ce = cudaStreamWaitEvent(copy_stream, ev, 0);
-        if (!ce)
-            ce = cudaMemcpyAsync((char *)host_out + (size_t)e0 * wave_bytes,
-                                 (const char *)out + (size_t)e0 * wave_bytes,
-                                 (size_t)ne * wave_bytes,
-                                 cudaMemcpyDeviceToHost, copy_stream);
+        if (!ce) {
+            const size_t pitch = (size_t)d->Nx * elem;
+            cudaMemcpy3DParms cp;
+            memset(&cp, 0, sizeof cp);
+            cp.srcPtr = make_cudaPitchedPtr(out, pitch, d->Nx, d->Ny);
+            cp.dstPtr = make_cudaPitchedPtr(host_out, pitch, d->Nx, d->Ny);
+            cp.srcPos = make_cudaPos(0, (size_t)r0, 0);
+            cp.dstPos = make_cudaPos(0, (size_t)r0, 0);
+            cp.extent = make_cudaExtent(pitch, (size_t)nr, (size_t)d->n_e);
+            cp.kind = cudaMemcpyDeviceToHost;
+            ce = cudaMemcpy3DAsync(&cp, copy_stream);
+        }
         cudaEventDestroy(ev);
         return ce ? cuda_status(ce, "exit-wave copy") : DYFOX_OK;
     };
@@ -689,10 +697,14 @@ static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
         }
     }
     laue_mark(1, stream);
+    // the rows outside the beam (zero) go to the host at once
+    if ((st = copy_rows(0, p.row0))) return st;
+    if ((st = copy_rows(p.row0 + p.n_rows, d->Ny - p.row0 - p.n_rows)))
+        return st;
     if (p.n_rows == 0) {
         laue_mark(2, stream);
         laue_mark(3, stream);
-        return copy_out(0, d->n_e);
+        return DYFOX_OK;
     }
     if (p.stage) {
         e = launch_cs_stage(single, (d->flags & DYFOX_FLAG_H_FP64) != 0,
@@ -730,7 +742,7 @@ static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
         }
         if ((e = cudaGetLastError())) return cuda_status(e, "laue_general");
         laue_mark(3, stream);
-        return copy_out(0, d->n_e);
+        return copy_rows(p.row0, p.n_rows);
     }
 
     FastConfig fc;
@@ -742,27 +754,24 @@ static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
     a.ncols = 32 * fc.WA * fc.cpl;
     a.stage = fc.stage;
     a.raw_elem = fc.raw_elem;
-    // Angles per march launch: all of them, or (copies to the host) a
-    // multiple of the angles a CTA takes (of pairs' angles for the pair
-    // march), so that every batch but the last fills its CTAs.
-    const int unit = fc.pairs ? 2 * fc.A : fc.A;
-    int nb = d->n_e;
-    if (host_out && march_batch > 0 && march_batch < d->n_e)
-        nb = div_up(march_batch, unit) * unit;
-    for (int e0 = 0; e0 < d->n_e; e0 += nb) {
-        const int ne = d->n_e - e0 < nb ? d->n_e - e0 : nb;
-        MarchArgs ab = a;
-        ab.n_e = ne;
-        ab.kappa = a.kappa + (size_t)e0 * nsteps;
-        ab.kappa32 = a.kappa32 + (size_t)e0 * nsteps;
-        ab.scale = a.scale + e0;
-        ab.out = (char *)out + (size_t)e0 * wave_bytes;
-        if (a.kpair) ab.kpair = a.kpair + (size_t)(e0 / 2) * nsteps * 4;
-        ab.n_groups = div_up(fc.pairs ? (ne + 1) / 2 : ne, fc.A);
-        e = fc.entry.launch(ab, p.n_rows * ab.n_groups, fc.block, fc.smem,
-                            stream);
+    a.n_groups = div_up(fc.pairs ? (d->n_e + 1) / 2 : d->n_e, fc.A);
+    // Row chunks (copies to the host), else one launch; the row-relative
+    // tables (staged e^{iH}, pivots) start at the chunk's first row.
+    int nc = host_out ? (n_chunks > 0 ? n_chunks : 8) : 1;
+    if (nc > 64) nc = 64;
+    if (nc > p.n_rows / 8) nc = p.n_rows / 8 > 1 ? p.n_rows / 8 : 1;
+    const int rc = div_up(p.n_rows, nc);
+    const size_t stage_row = (size_t)nsteps * d->Nx * elem;
+    for (int r0 = 0; r0 < p.n_rows; r0 += rc) {
+        const int nr = p.n_rows - r0 < rc ? p.n_rows - r0 : rc;
+        MarchArgs ac = a;
+        ac.row0 = p.row0 + r0;
+        ac.n_rows = nr;
+        if (p.stage) ac.csgrid = ws + p.off_stage + (size_t)r0 * stage_row;
+        ac.piv = a.piv + (size_t)r0 * nsteps * d->n_seg;
+        e = fc.entry.launch(ac, nr * ac.n_groups, fc.block, fc.smem, stream);
         if (e) return cuda_status(e, "laue_march");
-        if ((st = copy_out(e0, ne))) return st;
+        if ((st = copy_rows(p.row0 + r0, nr))) return st;
     }
     laue_mark(3, stream);
     return DYFOX_OK;
@@ -779,7 +788,7 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
 extern "C" int dyfox_laue_solve_to_host(
     const dyfox_laue_desc *d, const double *s_dev, const void *h_grid,
     const double *seg_table, void *out, void *host_out, void *workspace,
-    size_t workspace_bytes, int march_batch, void *stream,
+    size_t workspace_bytes, int n_chunks, void *stream,
     void *copy_stream) {
     if (!host_out) {
         set_error("host_out must be host memory (pinned for the copies to "
@@ -787,7 +796,7 @@ extern "C" int dyfox_laue_solve_to_host(
         return DYFOX_EINVAL;
     }
     return laue_solve_impl(d, s_dev, h_grid, seg_table, out, workspace,
-                           workspace_bytes, stream, host_out, march_batch,
+                           workspace_bytes, stream, host_out, n_chunks,
                            copy_stream ? (cudaStream_t)copy_stream
                                        : (cudaStream_t)stream);
 }

@@ -242,8 +242,9 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // e^{iH} (cos, sin) of column x in single precision from the segment
 // constants and the row's pivots.  HT_SEG: float-float sum started at the
-// reduced constant hcr, reduced mod 2 pi in float-float; HT_SEG64: double
-// sum started at the constant hconst, reduced in double.
+// reduced constant hcr, reduced mod 2 pi in float-float; HT_SEG64: the
+// segment terms summed exactly (seg_sum64), added to the constant hconst
+// and reduced in double.
 template <int HT>
 __device__ __forceinline__ float2 seg_phase_one(const SegF &f, float4 p0,
                                                 int x, float hcr,
@@ -256,7 +257,7 @@ __device__ __forceinline__ float2 seg_phase_one(const SegF &f, float4 p0,
         __sincosf(reduce_2pi_ff(hi, e), &sn, &c);
         return make_float2(c, sn);
     } else {
-        return CS<float>::of_f64(hconst + widen_f32(h));
+        return CS<float>::of_f64(seg_sum64(1, hconst, [&](int) { return h; }));
     }
 }
 
@@ -275,10 +276,9 @@ __device__ __forceinline__ float2 seg_phase(const SegF *segf,
         __sincosf(reduce_2pi_ff(hi, lo), &sn, &c);
         return make_float2(c, sn);
     } else {
-        double acc = hconst;
-        for (int s = 0; s < n_seg; ++s)
-            acc += widen_f32(h_seg_f32(segf[s], __ldg(pv + s), x));
-        return CS<float>::of_f64(acc);
+        return CS<float>::of_f64(seg_sum64(n_seg, hconst, [&](int s) {
+            return h_seg_f32(segf[s], __ldg(pv + s), x);
+        }));
     }
 }
 

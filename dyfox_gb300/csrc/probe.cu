@@ -94,7 +94,31 @@ __global__ void arith_probe64_kernel(int op, const double *__restrict__ a,
     }
 }
 
+// The FP64 segment sum (seg_sum64, constant 0) of each group of m floats
+// (dyfox_seg_sum_probe).
+__global__ void seg_sum_probe_kernel(const float *__restrict__ terms, int m,
+                                     double *out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *t = terms + (size_t)i * m;
+    out[i] = seg_sum64(m, 0.0, [&](int s) { return t[s]; });
+}
+
 }  // namespace dyfox
+
+extern "C" int dyfox_seg_sum_probe(const float *terms, int m, double *out,
+                                   int n, void *stream) {
+    dyfox::set_error("");
+    if (m < 0 || n < 0 || (n > 0 && (!out || (m > 0 && !terms)))) {
+        dyfox::set_error("bad arguments to dyfox_seg_sum_probe");
+        return DYFOX_EINVAL;
+    }
+    if (n == 0) return DYFOX_OK;
+    dyfox::seg_sum_probe_kernel<<<(n + 255) / 256, 256, 0,
+                                  (cudaStream_t)stream>>>(terms, m, out, n);
+    dyfox::count_launch(1);
+    return dyfox::cuda_status(cudaGetLastError(), "seg_sum_probe");
+}
 
 extern "C" int dyfox_arith_probe64(int op, const double *a, const double *b,
                                    double *out, int n, void *stream) {

@@ -194,13 +194,13 @@ def _solve(seg_list, s_dev_arr, grid, xtal, H_gpu, batch, precision,
                 _lib.ptr(table_dev), _lib.c_void_p(out[bs].data_ptr()),
                 _lib.ptr(ws), ws.numel(), stream), "dyfox_laue_solve")
         else:
-            # about eight march launches a call, each batch's waves copied
-            # while the next marches
+            # eight row chunks, each chunk's rows copied while the next
+            # marches
             _lib.check(_lib.lib().dyfox_laue_solve_to_host(
                 d, _lib.c_void_p(s_dev.data_ptr() + 8 * bs), _lib.ptr(H),
                 _lib.ptr(table_dev), _lib.c_void_p(out[bs].data_ptr()),
                 _lib.c_void_p(host_out[bs].data_ptr()), _lib.ptr(ws),
-                ws.numel(), max(1, (be - bs + 7) // 8), stream,
+                ws.numel(), 0, stream,
                 _lib.c_void_p(copy_stream.cuda_stream)),
                 "dyfox_laue_solve_to_host")
     if host_out is not None:

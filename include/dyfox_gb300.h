@@ -56,9 +56,13 @@ typedef enum dyfox_status {
 #define DYFOX_FLAG_NO_COMP 4u  /* FP32: plain (uncompensated) updates       */
 #define DYFOX_FLAG_GENERAL 8u  /* use the shared-memory general march even
                                   when shift_px == 1 (cross-checks)          */
-#define DYFOX_FLAG_H_FP64 16u  /* FP32 + H_SEGMENTS: sum the segment terms and
-                                  reduce mod 2 pi in double instead of in
-                                  float-float (two-sum) arithmetic           */
+#define DYFOX_FLAG_H_FP64 16u  /* FP32 + H_SEGMENTS: sum the segment terms
+                                  exactly (each rounded to 2^-44 rad; in
+                                  double, in order, where a term reaches
+                                  2^(18 - bit length of n_seg) rad, 2048
+                                  for 64 segments) and reduce mod 2 pi in
+                                  double, instead of in float-float
+                                  (two-sum) arithmetic                       */
 #define DYFOX_FLAG_PAIRS 32u   /* FP32 compensated, fused segments or staged
                                   e^{iH}, n_e >= 2: march two deviation
                                   parameters per thread in packed f32x2
@@ -140,18 +144,19 @@ int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
                      void *workspace, size_t workspace_bytes, void *stream);
 
 /* dyfox_laue_solve with the exit waves also copied into host memory while
- * the march proceeds: the march runs in batches of about march_batch
- * deviation parameters (rounded up to whole CTAs; 0 or >= n_e: one
- * batch), and after each batch its waves out[e0 .. e0 + nb) are copied
- * into host_out (same layout; pinned, for the copies to overlap) on
- * copy_stream (NULL: `stream`), behind an event on `stream`.  Returns
- * once the work is queued; host_out is complete when copy_stream is.  No
- * DYFOX counterpart (DYFOX returns device arrays): the copy of a
- * 256-angle scan's 1.2 GB of waves hides behind its march. */
+ * the march proceeds: the active rows are marched in n_chunks row chunks
+ * (0: 8; at most 64 and one per 8 rows), every deviation parameter in one
+ * launch per chunk, and after each chunk's march its rows of every wave
+ * are copied into host_out (same layout; pinned, for the copies to
+ * overlap) on copy_stream (NULL: `stream`), behind an event on `stream`;
+ * the rows outside the beam are copied at once.  Returns once the work is
+ * queued; host_out is complete when copy_stream is.  No DYFOX counterpart
+ * (DYFOX returns device arrays): the copy of a 256-angle scan's 1.2 GB of
+ * waves hides behind its march. */
 int dyfox_laue_solve_to_host(const dyfox_laue_desc *d, const double *s_dev,
                              const void *h_grid, const double *seg_table,
                              void *out, void *host_out, void *workspace,
-                             size_t workspace_bytes, int march_batch,
+                             size_t workspace_bytes, int n_chunks,
                              void *stream, void *copy_stream);
 
 /* dyfox_laue_solve for callers that cannot allocate device memory when
@@ -439,6 +444,12 @@ int dyfox_arith_probe(int op, const float *a, const float *b, void *out,
  * a, 5 __drcp_rn(a); n device doubles a (and b) into out. */
 int dyfox_arith_probe64(int op, const double *a, const double *b,
                         double *out, int n, void *stream);
+/* The FP64 segment sum of the FP32 march (the sum exact on a 2^-44 grid,
+ * or in double in order where a term is out of its range) over each of n
+ * groups of m device floats (terms, n * m of them) into n device doubles
+ * out. */
+int dyfox_seg_sum_probe(const float *terms, int m, double *out, int n,
+                        void *stream);
 
 /* Diagnostic (not part of any DYFOX interface): with on != 0, each later
  * dyfox_laue_solve on the calling thread records CUDA events on its stream

@@ -8,7 +8,9 @@ CUDA's correctly rounded operations, through dyfox_arith_probe:
   0 <= a <= b, the folded arguments of the atan2 polynomial: within 1 ulp;
 * the integer-built float-to-double widening of the FP64 segment sum
   against the hardware conversion: equal bit for bit, zeros, infinities,
-  NaN and subnormals included.
+  NaN and subnormals included;
+* the FP64 segment sum itself (exact on the 2^-66 grid, or in double in
+  order past its range) against the same sums formed exactly on the host.
 """
 
 import ctypes
@@ -139,3 +141,81 @@ def test_double_log_atan2_reciprocal_of_the_fp64_field(gpu):
     rm = _probe64(torch, 4, r2)
     rw = _probe64(torch, 5, r2)
     assert np.all(np.abs(rm - rw) <= np.spacing(np.abs(rw)))
+
+
+def _seg_sum(torch, terms):
+    from dyfox_gb300 import _lib
+    f = _lib.lib().dyfox_seg_sum_probe
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_int, ctypes.c_void_p]
+    n, m = terms.shape
+    t = torch.from_numpy(np.ascontiguousarray(terms, np.float32)).cuda()
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    _lib.check(f(t.data_ptr(), m, out.data_ptr(), n,
+                 torch.cuda.current_stream().cuda_stream),
+               "dyfox_seg_sum_probe")
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def _exact_grid_sum(row):
+    """Each float32 term split exactly into integers on the grids 1, 2^-22,
+    2^-44 and 2^-66 (each rounded to nearest, ties to even, from the
+    remainder of the coarser ones; float64 holds every remainder exactly),
+    the 1 and 2^-22 parts gathered in units of 2^-22, the others in units
+    of 2^-66, each total converted to double and the two added."""
+    hi = lo = 0
+    for h in row.astype(np.float64):
+        q = []
+        r = h
+        for k in (0, 22, 44, 66):
+            qi = float(np.rint(r * 2.0 ** k))
+            q.append(int(qi))
+            r = r - qi * 2.0 ** -k
+        hi += q[0] * 2 ** 22 + q[1]
+        lo += q[2] * 2 ** 22 + q[3]
+    return 0.0 + (float(hi) * 2.0 ** -22 + float(lo) * 2.0 ** -66)
+
+
+def _ordered_double_sum(row):
+    acc = 0.0
+    for h in row.astype(np.float64):
+        acc += h
+    return acc
+
+
+@pytest.mark.parametrize("m", [1, 7, 64, 700])
+def test_exact_segment_sum(gpu, m):
+    """seg_sum64 over groups of m terms of the sizes the Volterra phase
+    meets (magnitudes from 1e-9 to 1e3 rad, mixed signs, cancelling pairs,
+    exact ties of the grids): bit for bit the exact sum of the terms
+    rounded to the 2^-66 grid, rounded to double; groups with a term at or above the range limit
+    (2^(18 - bit length of m)), an infinity or a NaN: bit for bit the
+    in-order double sum."""
+    rng = np.random.default_rng(11 + m)
+    n = 512
+    mag = 10.0 ** rng.uniform(-9, 3, (n, m))
+    t = (rng.choice([-1.0, 1.0], (n, m)) * mag).astype(np.float32)
+    t[1, :] = np.float32(1e-30)
+    if m >= 2:
+        t[2, 1] = -t[2, 0]                          # cancelling pair
+        t[3, :2] = [np.float32(2.0 ** -67), np.float32(3 * 2.0 ** -67)]
+        t[4, :2] = [np.float32(1 + 2.0 ** -23), np.float32(0.5)]
+    limit = 2.0 ** (18 - int(m).bit_length())
+    over = [5, 6, 7, 8]
+    t[5, 0] = np.float32(limit)                     # at the limit
+    t[6, -1] = np.float32(-4 * limit)
+    t[7, 0] = np.inf
+    t[8, 0] = np.nan
+    for i in range(n):
+        if i not in over:
+            t[i] = np.clip(t[i], -limit / 2, limit / 2)
+    got = _seg_sum(gpu, t)
+    for i in range(n):
+        want = (_ordered_double_sum(t[i]) if i in over
+                else _exact_grid_sum(t[i]))
+        if np.isnan(want):
+            assert np.isnan(got[i]), i
+        else:
+            assert got[i] == want, (i, got[i], want)

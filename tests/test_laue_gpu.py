@@ -352,13 +352,13 @@ def test_fused_and_staged_phase_agree_bitwise(gpu, diamond400, small_grid,
                                               ("fp32", "fused", False),
                                               ("fp32", "staged", True),
                                               ("fp64", "auto", False)])
-def test_host_out_copies_every_angle_batch(gpu, diamond400, small_grid, rng,
-                                           prec, h_mode, pairs):
-    """host_out: the march in batches of angles with each batch's waves
-    copied to pinned host memory while the next marches gives the device
-    call's bytes, for angle counts that leave a short last batch, through
-    the scalar and the pair march and in FP64; a host_out of the wrong
-    shape is refused."""
+def test_host_out_copies_every_row_chunk(gpu, diamond400, small_grid, rng,
+                                         prec, h_mode, pairs):
+    """host_out: the march in row chunks with each chunk's rows of every
+    wave copied to pinned host memory while the next marches (and the rows
+    outside the beam copied at once) gives the device call's bytes, for
+    several angle counts, through the scalar and the pair march and in
+    FP64; a host_out of the wrong shape is refused."""
     from dyfox_gb300.laue import _solve, solve_dislocation
     torch = gpu
     segs = random_segments(diamond400, small_grid, 3, rng)
