@@ -57,10 +57,10 @@ typedef enum dyfox_status {
 #define DYFOX_FLAG_GENERAL 8u  /* use the shared-memory general march even
                                   when shift_px == 1 (cross-checks)          */
 #define DYFOX_FLAG_H_FP64 16u  /* FP32 + H_SEGMENTS: sum the segment terms
-                                  exactly (each rounded to 2^-44 rad; in
-                                  double, in order, where a term reaches
-                                  2^(18 - bit length of n_seg) rad, 2048
-                                  for 64 segments) and reduce mod 2 pi in
+                                  exactly (each rounded to 2^-66 rad) and
+                                  round the total to double (in double, in
+                                  order, where the terms' magnitudes sum to
+                                  2^17 rad or more) and reduce mod 2 pi in
                                   double, instead of in float-float
                                   (two-sum) arithmetic                       */
 #define DYFOX_FLAG_PAIRS 32u   /* FP32 compensated, fused segments or staged
@@ -444,8 +444,8 @@ int dyfox_arith_probe(int op, const float *a, const float *b, void *out,
  * a, 5 __drcp_rn(a); n device doubles a (and b) into out. */
 int dyfox_arith_probe64(int op, const double *a, const double *b,
                         double *out, int n, void *stream);
-/* The FP64 segment sum of the FP32 march (the sum exact on a 2^-44 grid,
- * or in double in order where a term is out of its range) over each of n
+/* The FP64 segment sum of the FP32 march (the sum exact on a 2^-66 grid
+ * rounded to double, or in double in order past its range) over each of n
  * groups of m device floats (terms, n * m of them) into n device doubles
  * out. */
 int dyfox_seg_sum_probe(const float *terms, int m, double *out, int n,

@@ -190,27 +190,25 @@ def test_exact_segment_sum(gpu, m):
     """seg_sum64 over groups of m terms of the sizes the Volterra phase
     meets (magnitudes from 1e-9 to 1e3 rad, mixed signs, cancelling pairs,
     exact ties of the grids): bit for bit the exact sum of the terms
-    rounded to the 2^-66 grid, rounded to double; groups with a term at or above the range limit
-    (2^(18 - bit length of m)), an infinity or a NaN: bit for bit the
+    rounded to the 2^-66 grid, rounded to double; groups whose magnitudes
+    sum to 2^17 rad or more, or with an infinity or a NaN: bit for bit the
     in-order double sum."""
     rng = np.random.default_rng(11 + m)
     n = 512
     mag = 10.0 ** rng.uniform(-9, 3, (n, m))
     t = (rng.choice([-1.0, 1.0], (n, m)) * mag).astype(np.float32)
+    cap = np.float32(2.0 ** 16 / m)                 # sum of |h| below 2^16
+    t = np.clip(t, -cap, cap)
     t[1, :] = np.float32(1e-30)
     if m >= 2:
         t[2, 1] = -t[2, 0]                          # cancelling pair
         t[3, :2] = [np.float32(2.0 ** -67), np.float32(3 * 2.0 ** -67)]
         t[4, :2] = [np.float32(1 + 2.0 ** -23), np.float32(0.5)]
-    limit = 2.0 ** (18 - int(m).bit_length())
     over = [5, 6, 7, 8]
-    t[5, 0] = np.float32(limit)                     # at the limit
-    t[6, -1] = np.float32(-4 * limit)
+    t[5, 0] = np.float32(2.0 ** 17)                 # at the limit
+    t[6, -1] = np.float32(-2.0 ** 19)
     t[7, 0] = np.inf
     t[8, 0] = np.nan
-    for i in range(n):
-        if i not in over:
-            t[i] = np.clip(t[i], -limit / 2, limit / 2)
     got = _seg_sum(gpu, t)
     for i in range(n):
         want = (_ordered_double_sum(t[i]) if i in over
