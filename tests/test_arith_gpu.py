@@ -191,8 +191,8 @@ def test_exact_segment_sum(gpu, m):
     meets (magnitudes from 1e-9 to 1e3 rad, mixed signs, cancelling pairs,
     exact ties of the grids): bit for bit the exact sum of the terms
     rounded to the 2^-66 grid, rounded to double; groups whose magnitudes
-    sum to 2^17 rad or more, or with an infinity or a NaN: bit for bit the
-    in-order double sum."""
+    sum to 2^17 rad or more, or with an infinity or a NaN, and single
+    terms: bit for bit the in-order double sum."""
     rng = np.random.default_rng(11 + m)
     n = 512
     mag = 10.0 ** rng.uniform(-9, 3, (n, m))
@@ -211,7 +211,7 @@ def test_exact_segment_sum(gpu, m):
     t[8, 0] = np.nan
     got = _seg_sum(gpu, t)
     for i in range(n):
-        want = (_ordered_double_sum(t[i]) if i in over
+        want = (_ordered_double_sum(t[i]) if i in over or m == 1
                 else _exact_grid_sum(t[i]))
         if np.isnan(want):
             assert np.isnan(got[i]), i
