@@ -269,7 +269,8 @@ __device__ __forceinline__ float2 seg_phase(const SegF *segf,
         float hi = hcr, lo = 0.0f;
         for (int s = 0; s < n_seg; ++s) {
             float e;
-            hi = two_sum(hi, h_seg_f32(segf[s], __ldg(pv + s), x), e);
+            hi = two_sum(hi, h_seg_f32(load_segf(segf + s), __ldg(pv + s), x),
+                         e);
             lo += e;
         }
         float sn, c;
@@ -277,7 +278,7 @@ __device__ __forceinline__ float2 seg_phase(const SegF *segf,
         return make_float2(c, sn);
     } else {
         return CS<float>::of_f64(seg_sum64(n_seg, hconst, [&](int s) {
-            return h_seg_f32(segf[s], __ldg(pv + s), x);
+            return h_seg_f32(load_segf(segf + s), __ldg(pv + s), x);
         }));
     }
 }

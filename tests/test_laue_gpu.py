@@ -380,6 +380,51 @@ def test_host_out_copies_every_row_chunk(gpu, diamond400, small_grid, rng,
                           **kw)
 
 
+@pytest.mark.parametrize("n_chunks", [1, 3, 1000])
+def test_host_copy_row_chunks_through_the_c_abi(gpu, diamond400, small_grid,
+                                                rng, n_chunks):
+    """dyfox_laue_solve_to_host with an explicit row-chunk count (one, a
+    count that leaves a short last chunk, and more than the rows allow,
+    which the library caps): host_out and out hold the bytes of
+    dyfox_laue_solve."""
+    from dyfox_gb300 import _lib
+    from dyfox_gb300.grid import grid_arrays
+    from dyfox_gb300.laue import _desc
+    from dyfox_gb300.backend import precision as as_precision
+    torch = gpu
+    segs = random_segments(diamond400, small_grid, 3, rng)
+    geo = grid_arrays(small_grid)
+    s = np.linspace(-3e5, 3e5, 7)
+    p = as_precision("fp32")
+    table = _lib.segment_table(segs, diamond400.g_vec, diamond400.nu,
+                               diamond400.a_core, geo["dx"])
+    tdev = _lib.device_table(table)
+    s_dev = torch.from_numpy(s).cuda()
+    d = _desc(diamond400, geo, len(s), p, _lib.H_SEGMENTS, len(table),
+              flags=_lib.FLAG_STAGED | _lib.FLAG_H_FP64)
+    ws = torch.empty(_lib.lib().dyfox_laue_workspace_bytes(d),
+                     dtype=torch.uint8, device="cuda")
+    shape = (len(s), geo["Ny"], geo["Nx"])
+    stream = torch.cuda.current_stream()
+    want = torch.empty(shape, dtype=p.torch_complex, device="cuda")
+    _lib.check(_lib.lib().dyfox_laue_solve(
+        d, _lib.ptr(s_dev), None, _lib.ptr(tdev), _lib.ptr(want),
+        _lib.ptr(ws), ws.numel(), _lib.c_void_p(stream.cuda_stream)),
+        "dyfox_laue_solve")
+    out = torch.full(shape, float("nan"), dtype=p.torch_complex,
+                     device="cuda")
+    host = torch.full(shape, float("nan"), dtype=p.torch_complex,
+                      pin_memory=True)
+    _lib.check(_lib.lib().dyfox_laue_solve_to_host(
+        d, _lib.ptr(s_dev), None, _lib.ptr(tdev), _lib.ptr(out),
+        _lib.c_void_p(host.data_ptr()), _lib.ptr(ws), ws.numel(), n_chunks,
+        _lib.c_void_p(stream.cuda_stream), None), "dyfox_laue_solve_to_host")
+    torch.cuda.synchronize()
+    w = np_(want)
+    assert np_(out).tobytes() == w.tobytes()
+    assert host.numpy().tobytes() == w.tobytes()
+
+
 @pytest.mark.parametrize("h_mode,h_sum", [("fused", "ff"),
                                            ("fused", "fp64"),
                                            ("staged", "ff")])
