@@ -60,7 +60,7 @@ README_WORKLOAD = ("laue-readme: diamond(400) 17 keV, t=200um dx=0.25um "
 # laue_march_kernel<float, 11, staged e^{iH}, compensated>: an ncu capture
 # of the full 256-angle launch (`python bench.py --once scan256`: the staged
 # e^{iH} table, 2.0 GB, read once, and the 1.0 GB of exit waves written).
-MARCH_SCAN_DRAM_BYTES = 2008256768 + 1023303936
+MARCH_SCAN_DRAM_BYTES = 2011342592 + 1023207424
 MARCH_SCAN_DRAM_SHAPE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum "
                          "of the 256-angle march launch (11 columns per "
                          "lane, 4 angles per CTA: the block's register "
@@ -268,6 +268,14 @@ class LaueCall:
             _lib.ptr(self.out), _lib.ptr(self.ws), self.ws.numel(),
             _lib.c_void_p(self.stream.cuda_stream)), "dyfox_laue_solve")
 
+    def check(self):
+        """Raises if the last call's bounded device waits ran out."""
+        from dyfox_gb300 import _lib
+        _lib.check(self.L.dyfox_laue_solve_status(
+            self.d, _lib.ptr(self.ws), self.ws.numel(),
+            _lib.c_void_p(self.stream.cuda_stream)),
+            "dyfox_laue_solve_status")
+
 
 def timed_steps(fn, steps, warmup, flush, kernel_ms=False):
     """Device time (ms) of each of ``steps`` calls after ``warmup``, CUDA
@@ -367,6 +375,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    chosen.check()
     tot = max_over_ranks(sum(ms) / 1e3, world)
     value = world * units * args.steps / tot
     mean_ms = 1e3 * tot / args.steps

@@ -14,6 +14,7 @@ from .build import LIB
 
 DYFOX_OK, DYFOX_EINVAL, DYFOX_ENOMEM, DYFOX_ESMEM = 0, 1, 2, 3
 DYFOX_EMAXITER, DYFOX_ENAN, DYFOX_ECUDA, DYFOX_ENOSYS = 4, 5, 6, 7
+DYFOX_ETIMEOUT = 8
 DYFOX_FP64, DYFOX_FP32 = 0, 1
 H_NONE, H_GRID_F64, H_GRID_F32, H_SEGMENTS, H_ANALYTIC = 0, 1, 2, 3, 4
 FLAG_FUSED, FLAG_STAGED, FLAG_NO_COMP, FLAG_GENERAL = 1, 2, 4, 8
@@ -29,7 +30,7 @@ class DyfoxError(RuntimeError):
 _EXC = {DYFOX_EINVAL: ValueError, DYFOX_ENOMEM: MemoryError,
         DYFOX_ESMEM: MemoryError, DYFOX_EMAXITER: DyfoxError,
         DYFOX_ENAN: ValueError, DYFOX_ECUDA: DyfoxError,
-        DYFOX_ENOSYS: NotImplementedError}
+        DYFOX_ENOSYS: NotImplementedError, DYFOX_ETIMEOUT: DyfoxError}
 
 c_int, c_uint, c_double, c_size_t, c_void_p = (
     ctypes.c_int, ctypes.c_uint, ctypes.c_double, ctypes.c_size_t,
@@ -75,6 +76,8 @@ _SIGNATURES = {
                                          c_void_p, c_void_p, c_void_p,
                                          c_void_p, c_void_p, c_size_t,
                                          c_int, c_void_p, c_void_p]),
+    "dyfox_laue_solve_status": (c_int, [ctypes.POINTER(LaueDesc), c_void_p,
+                                        c_size_t, c_void_p]),
 }
 
 _lib = None

@@ -56,6 +56,7 @@ _SIG = {
         ctypes.POINTER(_lib.c_void_p)]),
     "dyfox_batch_launch": (_lib.c_int, [_lib.c_void_p, _lib.c_void_p]),
     "dyfox_batch_kernel_count": (_lib.c_int, [_lib.c_void_p]),
+    "dyfox_batch_status": (_lib.c_int, [_lib.c_void_p, _lib.c_void_p]),
     "dyfox_batch_destroy": (_lib.c_int, [_lib.c_void_p]),
 }
 _bound = False
@@ -218,6 +219,14 @@ class Batch:
         _lib.check(_L().dyfox_batch_launch(self._handle, _lib.stream_ptr()),
                    "dyfox_batch_launch")
         return self.outputs
+
+    def check(self):
+        """Waits for the last run on torch's current stream and raises
+        DyfoxError if one of its bounded device waits ran out."""
+        if self._handle is None:
+            raise ValueError("batch is closed")
+        _lib.check(_L().dyfox_batch_status(self._handle, _lib.stream_ptr()),
+                   "dyfox_batch_status")
 
     def close(self):
         if getattr(self, "_handle", None) is not None:

@@ -105,6 +105,10 @@ laue_batch_kernel(const LaueInst *__restrict__ insts,
                 stage_chunk32(a.segs, a.n_seg, a.Nx, a.Ny, a.dx, a.dz, a.row0,
                               k0, kn, s_sum64 != 0, slab, smem);
             }
+            // the slab, written here through the generic proxy, is read by
+            // the march's bulk copies (async proxy)
+            asm volatile("fence.proxy.async.global;" ::: "memory");
+            __syncthreads();
         }
         // staged rows: the march specialised for them at compile time
         for (int g = 0; g < a.n_groups; ++g) {
@@ -333,7 +337,8 @@ static int batch_plan(const dyfox_batch_item *items, int n,
     }
     L->off_linst = off; off = al256(off + L->laue.size() * sizeof(LaueInst));
     L->off_items = off; off = al256(off + (size_t)L->n_items * sizeof(int2));
-    L->off_ticket = off; off = al256(off + sizeof(int));
+    // [0] the item ticket, [1] the march's wait status
+    L->off_ticket = off; off = al256(off + 2 * sizeof(int));
     L->off_slabs = off;
     off = al256(off + (size_t)L->grid * L->slab_elems * sizeof(float2));
     L->off_binst = off; off = al256(off + L->bragg.size() * sizeof(BraggArgs));
@@ -351,6 +356,7 @@ struct dyfox_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int kernels = 0;
+    const int *err = nullptr;   // the march's wait status in the workspace
 };
 
 using namespace dyfox;
@@ -378,7 +384,7 @@ static int record_batch(const dyfox_batch_item *items, const BatchLayout &L,
                         std::vector<BraggArgs> *bargs) {
     cudaError_t e;
     int st;
-    if ((e = cudaMemsetAsync(ws + L.off_ticket, 0, sizeof(int), s)))
+    if ((e = cudaMemsetAsync(ws + L.off_ticket, 0, 2 * sizeof(int), s)))
         return cuda_status(e, "ticket reset");
     for (const LaueB &b : L.laue) {
         const dyfox_laue_desc *d = &items[b.item].laue;
@@ -474,6 +480,7 @@ extern "C" int dyfox_batch_create(const dyfox_batch_item *items, int n,
         a.out = it.out;
         a.stage = seg ? ST_DIRECT : ST_COMPUTE;
         a.raw_elem = seg ? 8 : 0;
+        a.err = (int *)(ws + L.off_ticket) + 1;
         linst[j].sum64 = (d->flags | o.flags) & DYFOX_FLAG_H_FP64 ? 1 : 0;
         const double nsteps = d->Nz - 1;
         const double cost = nsteps * (3.0 * a.n_seg * d->Nx +
@@ -569,6 +576,7 @@ extern "C" int dyfox_batch_create(const dyfox_batch_item *items, int n,
         return st ? st : cuda_status(e, "end capture");
     }
     b->graph = g;
+    b->err = (const int *)(ws + L.off_ticket) + 1;
     // The Bragg instances' arguments, read by the graph's Bragg launches.
     if (!bargs.empty()) {
         e = cudaMemcpyAsync(ws + L.off_binst, bargs.data(),
@@ -595,6 +603,26 @@ extern "C" int dyfox_batch_launch(dyfox_batch *b, void *stream) {
     cudaError_t e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
     if (e) return cuda_status(e, "graph launch");
     count_launch((unsigned)b->kernels);
+    return DYFOX_OK;
+}
+
+extern "C" int dyfox_batch_status(const dyfox_batch *b, void *stream) {
+    set_error("");
+    if (!b || !b->err) {
+        set_error("NULL batch");
+        return DYFOX_EINVAL;
+    }
+    int err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, b->err, sizeof(int),
+                                    cudaMemcpyDeviceToHost,
+                                    (cudaStream_t)stream);
+    if (!e) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e) return cuda_status(e, "batch status");
+    if (err) {
+        set_error("a staged row's copy into shared memory did not complete "
+                  "within its bounded wait; its exit waves read NaN");
+        return DYFOX_ETIMEOUT;
+    }
     return DYFOX_OK;
 }
 

@@ -245,10 +245,12 @@ struct PrologueArgs {
     // pivots
     const double *segs; int n_seg, Nx; double dx, dz; float4 *piv;
     int nz, ns, np;
+    int *err;                   // the march's wait status, zeroed here
 };
 
 __global__ void laue_prologue_kernel(const PrologueArgs a) {
     const int b = blockIdx.x;
+    if (b == 0 && threadIdx.x == 0 && a.err) *a.err = 0;
     if (b < a.nz) {
         zero_rows_blocks(a.out, a.n_e, a.Ny, a.row_bytes, a.row0, a.n_rows, b,
                          a.nz);
@@ -272,7 +274,7 @@ struct LauePlan {
     int stage = 0;           // 0: none, 1: stage e^{iH} (CS32/CS64)
     int row0 = 0, n_rows = 0;
     size_t off_kappa = 0, off_k32 = 0, off_scale = 0, off_stage = 0,
-           off_piv = 0, off_kpair = 0, ws = 0;
+           off_piv = 0, off_kpair = 0, off_err = 0, ws = 0;
 };
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -384,6 +386,8 @@ static int make_plan(const dyfox_laue_desc *d, LauePlan *p) {
     if (single)
         off = align256(off + (size_t)((d->n_e + 1) / 2) * (d->Nz - 1) *
                                  sizeof(KPair));
+    p->off_err = off;
+    off = align256(off + sizeof(int));
     p->ws = off;
     return DYFOX_OK;
 }
@@ -634,6 +638,7 @@ static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
     a.csgrid = ws + p.off_stage;
     a.piv = (const float4 *)(ws + p.off_piv);
     a.kpair = single ? (const float4 *)(ws + p.off_kpair) : nullptr;
+    a.err = (int *)(ws + p.off_err);
 
     cudaError_t e;
     // Rows [r0, r0 + nr) of every angle of out into host_out on
@@ -679,6 +684,7 @@ static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
         pa.kpair = single ? (float *)(ws + p.off_kpair) : nullptr;
         pa.segs = seg_table; pa.n_seg = d->n_seg; pa.Nx = d->Nx;
         pa.dx = d->dx; pa.dz = d->dz; pa.piv = (float4 *)(ws + p.off_piv);
+        pa.err = (int *)(ws + p.off_err);
         const long zpairs = p.n_rows < d->Ny ? (long)d->n_e * (d->Ny - p.n_rows)
                                               : 0;
         pa.nz = (int)(zpairs < 152L * 16 ? zpairs : 152L * 16);
@@ -694,6 +700,8 @@ static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
             laue_prologue_kernel<<<blocks, 256, 0, stream>>>(pa);
             count_launch(1);
             if ((e = cudaGetLastError())) return cuda_status(e, "prologue");
+        } else if ((e = cudaMemsetAsync(pa.err, 0, sizeof(int), stream))) {
+            return cuda_status(e, "status reset");
         }
     }
     laue_mark(1, stream);
@@ -783,6 +791,31 @@ extern "C" int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
                                 size_t workspace_bytes, void *stream) {
     return laue_solve_impl(d, s_dev, h_grid, seg_table, out, workspace,
                            workspace_bytes, stream, nullptr, 0, nullptr);
+}
+
+extern "C" int dyfox_laue_solve_status(const dyfox_laue_desc *d,
+                                       const void *workspace,
+                                       size_t workspace_bytes, void *stream) {
+    set_error("");
+    LauePlan p;
+    int st = make_plan(d, &p);
+    if (st) return st;
+    if (!workspace || workspace_bytes < p.ws) {
+        set_error("workspace of %zu bytes, %zu needed", workspace_bytes, p.ws);
+        return DYFOX_ENOMEM;
+    }
+    int err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, (const char *)workspace + p.off_err,
+                                    sizeof(int), cudaMemcpyDeviceToHost,
+                                    (cudaStream_t)stream);
+    if (!e) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e) return cuda_status(e, "solve status");
+    if (err) {
+        set_error("a staged row's copy into shared memory did not complete "
+                  "within its bounded wait; its exit waves read NaN");
+        return DYFOX_ETIMEOUT;
+    }
+    return DYFOX_OK;
 }
 
 extern "C" int dyfox_laue_solve_to_host(

@@ -83,6 +83,8 @@ struct MarchArgs {
     void *out;                  // (n_e, Ny, Nx) complex (R2)
     int stage;                  // StageMode of a GENERIC source
     int raw_elem;               // bytes per column of a staged raw row
+    int *err;                   // set to 1 when a bounded wait ran out
+                                // (NULL: not recorded)
 };
 
 // Input beam D0(z=0) at column x (kernels.py:77-88), in double.
@@ -191,7 +193,7 @@ enum StageMode { ST_COMPUTE = 0, ST_DIRECT = 1, ST_CONVERT = 2 };
 // Rows use the natural column layout: element x of a row is column x; lane
 // L reads x = L * CPL + j (odd CPL keeps 8-byte reads conflict-free).
 struct MarchSmem {
-    size_t cs, raw, raw_stage, bnd, an, segf, hc, total;
+    size_t cs, raw, raw_stage, bnd, an, segf, hc, bars, total;
 };
 
 template <typename R>
@@ -222,8 +224,73 @@ __host__ __device__ inline MarchSmem march_smem(int CPL, int WA, int A,
     off = (off + 15) & ~(size_t)15;
     m.hc = off;
     off += sizeof(double);
+    // three mbarriers of the bulk row copies (direct staging)
+    off = (off + 7) & ~(size_t)7;
+    m.bars = off;
+    if (stage == ST_DIRECT) off += 3 * sizeof(unsigned long long);
     m.total = off;
     return m;
+}
+
+// One thread's bulk copy of a staged row (cp.async.bulk, completion counted
+// in bytes on an mbarrier) and the waits on it.  Both addresses 16-byte
+// aligned, bytes a multiple of 16 (the direct staging guarantees both).
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void row_bar_init(unsigned long long *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void row_bar_inval(unsigned long long *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_row(void *dst, const void *src,
+                                         unsigned bytes,
+                                         unsigned long long *bar) {
+    // the generic-proxy reads of this stage (ordered by the barrier that
+    // preceded) before the async-proxy write
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                     smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool row_bar_try(unsigned long long *bar,
+                                            unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the phase `parity` of bar, at most about 2 s of the global
+// timer; false when it gave up.
+static __device__ __noinline__ bool row_bar_wait_slow(unsigned long long *bar,
+                                               unsigned parity) {
+    unsigned long long t0, t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (unsigned it = 0;; ++it) {
+        if (row_bar_try(bar, parity)) return true;
+        if ((it & 255u) == 255u) {
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            if (t - t0 > 2000000000ull) return false;
+        }
+    }
+}
+__device__ __forceinline__ bool row_bar_wait(unsigned long long *bar,
+                                             unsigned parity) {
+    return row_bar_try(bar, parity) || row_bar_wait_slow(bar, parity);
 }
 
 __device__ __forceinline__ void cp_async16(void *dst_smem, const void *src) {
@@ -318,6 +385,12 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     R2 *an_cs = reinterpret_cast<R2 *>(smem + plan.an);
     SegF *segf = reinterpret_cast<SegF *>(smem + plan.segf);
     double *hc_sm = reinterpret_cast<double *>(smem + plan.hc);
+    unsigned long long *bars =
+        reinterpret_cast<unsigned long long *>(smem + plan.bars);
+    // staged rows arrive by one thread's bulk copy per step (an mbarrier a
+    // ring stage) instead of every thread's cp.async
+    constexpr bool kBulk = kStaged;
+    bool bulk_ok = true;
     const int NB = COMP ? 4 : 2;
     const double y_pix = (iy - a.Ny / 2) * a.dx;
 
@@ -330,6 +403,10 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     if (HT == HT_GENERIC && hsrc == HS_ANALYTIC) {
         for (int k = tid; k < nsteps; k += nthreads)
             an_cs[k] = CS<R>::of_f64(analytic_h(a.an, y_pix, k, a.dz));
+    }
+    if (kBulk && tid == 0) {
+        for (int st = 0; st < 3; ++st) row_bar_init(&bars[st]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (stage == ST_DIRECT) {
         // Columns beyond Nx of every stage read as zero coupling.
@@ -375,6 +452,13 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     const int chunks = (Nx * raw_elem) >> 4;
     // ring: the stage (kk % 3) of step kk, tracked by the caller.
     auto stage_issue = [&](int kk, int ring) {
+        if constexpr (kBulk) {
+            if (tid == 0 && kk < nsteps)
+                bulk_row(raw + (size_t)ring * plan.raw_stage,
+                         raw_src + (raw_row + kk) * (size_t)Nx * raw_elem,
+                         (unsigned)(Nx * raw_elem), &bars[ring]);
+            return;
+        }
         if (kk < nsteps) {
             const unsigned char *src =
                 raw_src + (raw_row + kk) * (size_t)Nx * raw_elem;
@@ -595,6 +679,9 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                              ? reinterpret_cast<const R2 *>(
                                    raw + (size_t)ring * plan.raw_stage)
                              : cs + (size_t)p * ncols) + L * CPL;
+        // the row of step k: the (k / 3)-th phase of its stage's barrier
+        if constexpr (kBulk)
+            bulk_ok &= row_bar_wait(&bars[ring], (unsigned)(k / 3) & 1u);
         R pbr = binr, pbi = bini, pblr = binlr, pbli = binli;
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
@@ -649,7 +736,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         }
         // The stage of step k + 1 (DIRECT) or k + 2 (CONVERT) is complete
         // and, after the barrier, visible to every thread.
-        if (stage == ST_DIRECT) cp_async_wait<1>();
+        if (stage == ST_DIRECT && !kBulk) cp_async_wait<1>();
         else if (stage == ST_CONVERT) cp_async_wait<0>();
         __syncthreads();
     };
@@ -669,7 +756,13 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
             ring = ring == 2 ? 0 : ring + 1;
         }
     }
-    if (stage != ST_COMPUTE) cp_async_wait<0>();
+    if (stage != ST_COMPUTE && !kBulk) cp_async_wait<0>();
+    // Every issued row was waited for inside its step (and every thread is
+    // past the last step's barrier): the barriers can be released for the
+    // next use of this shared memory.
+    if (kBulk && tid == 0)
+        for (int st = 0; st < 3; ++st) row_bar_inval(&bars[st]);
+    if (!bulk_ok && a.err) atomicExch(a.err, 1);
 
     // ---------------------------------------------------------- output
     if (ie_raw >= a.n_e) return;
@@ -681,6 +774,8 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         if (x < Nx) {
             double br = (double)Br[j], bi = (double)Bi[j];
             if constexpr (COMP) { br += (double)Blr[j]; bi += (double)Bli[j]; }
+            // a row copy that never completed: the wave reads NaN
+            if (!bulk_ok) br = bi = __longlong_as_double(0x7ff8000000000000LL);
             out[x] = R2{(R)(S.x * br - S.y * bi), (R)(S.x * bi + S.y * br)};
         }
     }

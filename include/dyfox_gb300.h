@@ -31,7 +31,9 @@ typedef enum dyfox_status {
     DYFOX_EMAXITER = 4,    /* iterative solve hit its iteration cap        */
     DYFOX_ENAN = 5,        /* non-finite value met                         */
     DYFOX_ECUDA = 6,       /* CUDA runtime error                           */
-    DYFOX_ENOSYS = 7       /* configuration not supported                  */
+    DYFOX_ENOSYS = 7,      /* configuration not supported                  */
+    DYFOX_ETIMEOUT = 8     /* a bounded device wait ran out (the kernel
+                              returned; its results are not valid)         */
 } dyfox_status;
 
 /* Precision of a march.  FP64: plain double everywhere (parity mode).
@@ -142,6 +144,15 @@ size_t dyfox_laue_workspace_bytes(const dyfox_laue_desc *d);
 int dyfox_laue_solve(const dyfox_laue_desc *d, const double *s_dev,
                      const void *h_grid, const double *seg_table, void *out,
                      void *workspace, size_t workspace_bytes, void *stream);
+
+/* Device status of the last dyfox_laue_solve or dyfox_laue_solve_to_host
+ * queued on `stream` with this workspace:
+ * synchronises `stream`, then DYFOX_OK, or DYFOX_ETIMEOUT when a staged
+ * row's copy into shared memory did not complete within its bounded wait
+ * (about 2 s; the march then wrote that row's exit waves as NaN and
+ * returned instead of waiting longer). */
+int dyfox_laue_solve_status(const dyfox_laue_desc *d, const void *workspace,
+                            size_t workspace_bytes, void *stream);
 
 /* dyfox_laue_solve with the exit waves also copied into host memory while
  * the march proceeds: the active rows are marched in n_chunks row chunks
@@ -315,6 +326,12 @@ int dyfox_batch_launch(dyfox_batch *batch, void *stream);
 
 /* Kernel launches one replay makes (the graph's kernel nodes). */
 int dyfox_batch_kernel_count(const dyfox_batch *batch);
+
+/* Device status of the last replay queued on `stream`: synchronises
+ * `stream`, then DYFOX_OK, or DYFOX_ETIMEOUT when a staged row's copy into
+ * shared memory did not complete within its bounded wait (that row's exit
+ * waves read NaN). */
+int dyfox_batch_status(const dyfox_batch *batch, void *stream);
 
 /* Frees the graph and the plan (not the workspace). */
 int dyfox_batch_destroy(dyfox_batch *batch);

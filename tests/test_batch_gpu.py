@@ -62,6 +62,7 @@ def test_batch_equals_single_calls(gpu, small_set, h_sum):
     torch = gpu
     b = Batch(from_workload(small_set), h_sum=h_sum)
     b.run()
+    b.check()          # every bounded wait of the replay completed
     torch.cuda.synchronize()
     for w, out, info in zip(small_set, b.outputs, b.infos):
         if w["kind"] == "laue":

@@ -419,6 +419,9 @@ def test_host_copy_row_chunks_through_the_c_abi(gpu, diamond400, small_grid,
         d, _lib.ptr(s_dev), None, _lib.ptr(tdev), _lib.ptr(out),
         _lib.c_void_p(host.data_ptr()), _lib.ptr(ws), ws.numel(), n_chunks,
         _lib.c_void_p(stream.cuda_stream), None), "dyfox_laue_solve_to_host")
+    _lib.check(_lib.lib().dyfox_laue_solve_status(
+        d, _lib.ptr(ws), ws.numel(), _lib.c_void_p(stream.cuda_stream)),
+        "dyfox_laue_solve_status")
     torch.cuda.synchronize()
     w = np_(want)
     assert np_(out).tobytes() == w.tobytes()
