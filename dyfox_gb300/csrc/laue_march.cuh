@@ -627,7 +627,9 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     // in the staged march, which runs the steps unrolled by three, so that
     // every shared-memory address of the step is a constant offset; a
     // run-time value in the other marches.
-    auto step = [&](const int k, auto rc) {
+    // phase: the parity of the ring stage's barrier for step k (k / 3 mod
+    // 2; the staged loop passes its unrolled round's parity).
+    auto step = [&](const int k, auto rc, unsigned phase) {
         const int ring = rc;
         const int ring2 = ring == 0 ? 2 : ring - 1;      // (k + 2) % 3
         const int nslot = ring == 2 ? 0 : ring + 1;      // (k + 1) % 3
@@ -635,7 +637,8 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         R k12r, k12i, k21r, k21i;
         if constexpr (kSingle) {
             k12r = kn32.x; k12i = kn32.y; k21r = kn32.z; k21i = kn32.w;
-            if (k + 1 < nsteps) kn32 = __ldg(kap32 + k + 1);
+            // the next step's couplings (the last step reloads its own)
+            kn32 = __ldg(kap32 + (k + 1 < nsteps ? k + 1 : k));
         } else {
             k12r = (R)kn.k12.x; k12i = (R)kn.k12.y;
             k21r = (R)kn.k21.x; k21i = (R)kn.k21.y;
@@ -680,8 +683,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                                    raw + (size_t)ring * plan.raw_stage)
                              : cs + (size_t)p * ncols) + L * CPL;
         // the row of step k: the (k / 3)-th phase of its stage's barrier
-        if constexpr (kBulk)
-            bulk_ok &= row_bar_wait(&bars[ring], (unsigned)(k / 3) & 1u);
+        if constexpr (kBulk) bulk_ok &= row_bar_wait(&bars[ring], phase);
         R pbr = binr, pbi = bini, pblr = binlr, pbli = binli;
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
@@ -724,15 +726,13 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                 Alr[j] = e0; Ali[j] = e1; Blr[j] = e2; Bli[j] = e3;
             }
         }
-        if (lane == 0) {
-            bnd[(nslot * nwarps + warp) * NB + 0] = R2{Ar[0], Ai[0]};
+        // lane 0 publishes its A(0), lane 31 its B(CPL - 1) (one branch)
+        if (is_first || is_last) {
+            R2 *slot = bnd + (nslot * nwarps + warp) * NB + (is_first ? 0 : 1);
+            slot[0] = is_first ? R2{Ar[0], Ai[0]} : R2{Br[CPL - 1], Bi[CPL - 1]};
             if constexpr (COMP)
-                bnd[(nslot * nwarps + warp) * NB + 2] = R2{Alr[0], Ali[0]};
-        }
-        if (lane == 31) {
-            bnd[(nslot * nwarps + warp) * NB + 1] = R2{Br[CPL - 1], Bi[CPL - 1]};
-            if constexpr (COMP)
-                bnd[(nslot * nwarps + warp) * NB + 3] = R2{Blr[CPL - 1], Bli[CPL - 1]};
+                slot[2] = is_first ? R2{Alr[0], Ali[0]}
+                                   : R2{Blr[CPL - 1], Bli[CPL - 1]};
         }
         // The stage of step k + 1 (DIRECT) or k + 2 (CONVERT) is complete
         // and, after the barrier, visible to every thread.
@@ -742,17 +742,18 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     };
     if constexpr (kStaged) {
         int k = 0;
-        for (; k + 3 <= nsteps; k += 3) {
-            step(k, RingIdx<0>{});
-            step(k + 1, RingIdx<1>{});
-            step(k + 2, RingIdx<2>{});
+        unsigned phase = 0;
+        for (; k + 3 <= nsteps; k += 3, phase ^= 1u) {
+            step(k, RingIdx<0>{}, phase);
+            step(k + 1, RingIdx<1>{}, phase);
+            step(k + 2, RingIdx<2>{}, phase);
         }
-        if (k < nsteps) step(k, RingIdx<0>{});
-        if (k + 1 < nsteps) step(k + 1, RingIdx<1>{});
+        if (k < nsteps) step(k, RingIdx<0>{}, phase);
+        if (k + 1 < nsteps) step(k + 1, RingIdx<1>{}, phase);
     } else {
         int ring = 0;
         for (int k = 0; k < nsteps; ++k) {
-            step(k, ring);
+            step(k, ring, 0u);
             ring = ring == 2 ? 0 : ring + 1;
         }
     }
