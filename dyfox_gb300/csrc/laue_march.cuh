@@ -627,6 +627,21 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
     // in the staged march, which runs the steps unrolled by three, so that
     // every shared-memory address of the step is a constant offset; a
     // run-time value in the other marches.
+    // Staged march: every ring stage's row and boundary-slot addresses,
+    // fixed for the whole march (the unrolled steps index them by their
+    // compile-time stage).
+    const R2 *st_src[3], *st_next[3], *st_prev[3];
+    R2 *st_own[3];
+    if constexpr (kStaged) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            st_src[r] = reinterpret_cast<const R2 *>(
+                            raw + (size_t)r * plan.raw_stage) + L * CPL;
+            st_next[r] = bnd + (r * nwarps + nb_next) * NB;
+            st_prev[r] = bnd + (r * nwarps + nb_prev) * NB;
+            st_own[r] = bnd + (r * nwarps + warp) * NB + (is_first ? 0 : 1);
+        }
+    }
     // phase: the parity of the ring stage's barrier for step k (k / 3 mod
     // 2; the staged loop passes its unrolled round's parity).
     auto step = [&](const int k, auto rc, unsigned phase) {
@@ -663,25 +678,38 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         // Every lane reads the same boundary slots (a broadcast) and lanes
         // 31 and 0 keep them by selection, with no branch.
         {
-            const R2 t = bnd[(ring * nwarps + nb_next) * NB + 0];
-            const R2 v = bnd[(ring * nwarps + nb_prev) * NB + 1];
+            const R2 *nxt, *prv;
+            if constexpr (kStaged) {
+                nxt = st_next[ring];
+                prv = st_prev[ring];
+            } else {
+                nxt = bnd + (ring * nwarps + nb_next) * NB;
+                prv = bnd + (ring * nwarps + nb_prev) * NB;
+            }
+            const R2 t = nxt[0];
+            const R2 v = prv[1];
             ainr = is_last ? (has_next ? t.x : R(0)) : ainr;
             aini = is_last ? (has_next ? t.y : R(0)) : aini;
             binr = is_first ? (has_prev ? v.x : R(0)) : binr;
             bini = is_first ? (has_prev ? v.y : R(0)) : bini;
             if constexpr (COMP) {
-                const R2 u = bnd[(ring * nwarps + nb_next) * NB + 2];
-                const R2 w = bnd[(ring * nwarps + nb_prev) * NB + 3];
+                const R2 u = nxt[2];
+                const R2 w = prv[3];
                 ainlr = is_last ? (has_next ? u.x : R(0)) : ainlr;
                 ainli = is_last ? (has_next ? u.y : R(0)) : ainli;
                 binlr = is_first ? (has_prev ? w.x : R(0)) : binlr;
                 binli = is_first ? (has_prev ? w.y : R(0)) : binli;
             }
         }
-        const R2 *src = (stage == ST_DIRECT
-                             ? reinterpret_cast<const R2 *>(
-                                   raw + (size_t)ring * plan.raw_stage)
-                             : cs + (size_t)p * ncols) + L * CPL;
+        const R2 *src;
+        if constexpr (kStaged) {
+            src = st_src[ring];
+        } else {
+            src = (stage == ST_DIRECT
+                       ? reinterpret_cast<const R2 *>(
+                             raw + (size_t)ring * plan.raw_stage)
+                       : cs + (size_t)p * ncols) + L * CPL;
+        }
         // the row of step k: the (k / 3)-th phase of its stage's barrier
         if constexpr (kBulk) bulk_ok &= row_bar_wait(&bars[ring], phase);
         R pbr = binr, pbi = bini, pblr = binlr, pbli = binli;
@@ -728,7 +756,11 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         }
         // lane 0 publishes its A(0), lane 31 its B(CPL - 1) (one branch)
         if (is_first || is_last) {
-            R2 *slot = bnd + (nslot * nwarps + warp) * NB + (is_first ? 0 : 1);
+            R2 *slot;
+            if constexpr (kStaged)
+                slot = st_own[nslot];
+            else
+                slot = bnd + (nslot * nwarps + warp) * NB + (is_first ? 0 : 1);
             slot[0] = is_first ? R2{Ar[0], Ai[0]} : R2{Br[CPL - 1], Bi[CPL - 1]};
             if constexpr (COMP)
                 slot[2] = is_first ? R2{Alr[0], Ali[0]}
