@@ -395,6 +395,7 @@ static int make_plan(const dyfox_laue_desc *d, LauePlan *p) {
 struct FastConfig {
     MarchEntry entry;
     int cpl, WA, A, block;
+    int regs = 0;            // registers per thread of the chosen kernel
     size_t smem;
     int stage = ST_COMPUTE, raw_elem = 0;
     bool pairs = false;      // A counts angle pairs
@@ -467,6 +468,7 @@ static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
     cudaFuncAttributes attr;
     cudaError_t e = fc->entry.attr(&attr);
     if (e != cudaSuccess) return cuda_status(e, "cudaFuncGetAttributes(march)");
+    fc->regs = attr.numRegs;
     int max_threads = attr.maxThreadsPerBlock < 1024 ? attr.maxThreadsPerBlock
                                                      : 1024;
     int cap = 512 < max_threads ? 512 : max_threads;
@@ -501,6 +503,30 @@ static int choose_fast(const dyfox_laue_desc *d, const LauePlan &p,
                              fc->stage, fc->raw_elem);
     fc->smem = sm.total;
     return DYFOX_OK;
+}
+
+// CTAs of the chosen march resident on the whole device (0 when unknown):
+// the blocks a multiprocessor holds by registers (allocated per warp in
+// units of 256), shared memory (1 KB reserved a block), threads and the
+// 32-block limit, times the multiprocessor count.
+static int resident_ctas(const FastConfig &fc) {
+    int dev = 0, sms = 0, smem_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm,
+                               cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                               dev) != cudaSuccess ||
+        fc.regs <= 0 || fc.block <= 0)
+        return 0;
+    const int warps = (fc.block + 31) / 32;
+    const int warp_regs = (fc.regs * 32 + 255) / 256 * 256;
+    int per = 65536 / (warp_regs * warps);
+    const int by_smem = (int)((size_t)smem_sm / (fc.smem + 1024));
+    if (by_smem < per) per = by_smem;
+    if (2048 / fc.block < per) per = 2048 / fc.block;
+    if (per > 32) per = 32;
+    return per > 0 ? per * sms : 0;
 }
 
 // Staging mode of a grid source: rows are copied with 16-byte cp.async, so
@@ -583,7 +609,8 @@ extern "C" size_t dyfox_laue_workspace_bytes(const dyfox_laue_desc *d) {
 }
 
 // The solve of dyfox_laue_solve and dyfox_laue_solve_to_host.  host_out
-// non-NULL: the active rows are marched in n_chunks row chunks (0: 8), all
+// non-NULL: the active rows are marched in n_chunks row chunks (0: about
+// 8, in whole waves of CTAs), all
 // deviation parameters in one launch per chunk, and after each chunk's
 // march its rows of every wave are copied into host_out on copy_stream,
 // behind an event on `stream`.
@@ -768,7 +795,21 @@ static int laue_solve_impl(const dyfox_laue_desc *d, const double *s_dev,
     int nc = host_out ? (n_chunks > 0 ? n_chunks : 8) : 1;
     if (nc > 64) nc = 64;
     if (nc > p.n_rows / 8) nc = p.n_rows / 8 > 1 ? p.n_rows / 8 : 1;
-    const int rc = div_up(p.n_rows, nc);
+    int rc = div_up(p.n_rows, nc);
+    if (nc > 1 && n_chunks <= 0) {
+        // Chunks of whole waves of CTAs (the remainder rows last, so that
+        // the copy left after the march is short).
+        const int wave = resident_ctas(fc);
+        if (wave > 0) {
+            int g = a.n_groups, w = wave;
+            while (w) { const int t = g % w; g = w; w = t; }
+            const int unit = wave / g;           // rows per whole wave
+            if (unit <= p.n_rows / 4) {
+                const int want = p.n_rows / nc;
+                rc = unit * (want / unit > 0 ? want / unit : 1);
+            }
+        }
+    }
     const size_t stage_row = (size_t)nsteps * d->Nx * elem;
     for (int r0 = 0; r0 < p.n_rows; r0 += rc) {
         const int nr = p.n_rows - r0 < rc ? p.n_rows - r0 : rc;

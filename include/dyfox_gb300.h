@@ -156,8 +156,9 @@ int dyfox_laue_solve_status(const dyfox_laue_desc *d, const void *workspace,
 
 /* dyfox_laue_solve with the exit waves also copied into host memory while
  * the march proceeds: the active rows are marched in n_chunks row chunks
- * (0: 8; at most 64 and one per 8 rows), every deviation parameter in one
- * launch per chunk, and after each chunk's march its rows of every wave
+ * (at most 64 and one per 8 rows; 0: about 8, each a whole number of
+ * waves of resident CTAs with the remainder rows last), every deviation
+ * parameter in one launch per chunk, and after each chunk's march its rows of every wave
  * are copied into host_out (same layout; pinned, for the copies to
  * overlap) on copy_stream (NULL: `stream`), behind an event on `stream`;
  * the rows outside the beam are copied at once.  Returns once the work is
