@@ -380,6 +380,53 @@ def test_host_out_copies_every_row_chunk(gpu, diamond400, small_grid, rng,
                           **kw)
 
 
+@pytest.mark.parametrize("t_um", [0.5, 1.0, 1.8, 2.5, 3.0, 3.6])
+def test_staged_march_of_a_few_depth_steps(gpu, diamond400, rng, t_um):
+    """The staged march's ring of three row stages (one bulk copy a step,
+    an mbarrier phase a stage) at 1 to 6 depth steps, where the unrolled
+    rounds of three leave 0, 1 or 2 steps over: the bytes of the fused
+    march, in FP32 with both segment sums and in FP64, every bounded wait
+    completed."""
+    from dyfox_gb300 import _lib
+    from dyfox_gb300.grid import LaueGrid, grid_arrays
+    from dyfox_gb300.laue import _desc
+    from dyfox_gb300.backend import precision as as_precision
+    torch = gpu
+    grid = LaueGrid(diamond400, t_um * 1e-6, 0.25e-6, 4e-6,
+                    beam_thickness=1e-6)
+    geo = grid_arrays(grid)
+    segs = random_segments(diamond400, grid, 3, rng)
+    s = np.linspace(-3e5, 3e5, 5)
+    for prec, hflag in (("fp32", _lib.FLAG_H_FP64), ("fp32", 0),
+                        ("fp64", 0)):
+        p = as_precision(prec)
+        table = _lib.segment_table(segs, diamond400.g_vec, diamond400.nu,
+                                   diamond400.a_core, geo["dx"])
+        tdev = _lib.device_table(table)
+        s_dev = torch.from_numpy(s).cuda()
+        outs = []
+        for mode in (_lib.FLAG_FUSED, _lib.FLAG_STAGED):
+            d = _desc(diamond400, geo, len(s), p, _lib.H_SEGMENTS,
+                      len(table), flags=mode | hflag)
+            ws = torch.empty(_lib.lib().dyfox_laue_workspace_bytes(d),
+                             dtype=torch.uint8, device="cuda")
+            out = torch.full((len(s), geo["Ny"], geo["Nx"]), float("nan"),
+                             dtype=p.torch_complex, device="cuda")
+            stream = torch.cuda.current_stream()
+            _lib.check(_lib.lib().dyfox_laue_solve(
+                d, _lib.ptr(s_dev), None, _lib.ptr(tdev), _lib.ptr(out),
+                _lib.ptr(ws), ws.numel(),
+                _lib.c_void_p(stream.cuda_stream)), "dyfox_laue_solve")
+            _lib.check(_lib.lib().dyfox_laue_solve_status(
+                d, _lib.ptr(ws), ws.numel(),
+                _lib.c_void_p(stream.cuda_stream)),
+                "dyfox_laue_solve_status")
+            outs.append(np_(out))
+        assert geo["Nz"] >= 2
+        assert np.isfinite(outs[1]).all(), (prec, geo["Nz"])
+        assert outs[0].tobytes() == outs[1].tobytes(), (prec, geo["Nz"])
+
+
 @pytest.mark.parametrize("n_chunks", [1, 3, 1000])
 def test_host_copy_row_chunks_through_the_c_abi(gpu, diamond400, small_grid,
                                                 rng, n_chunks):
