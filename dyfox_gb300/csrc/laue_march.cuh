@@ -183,10 +183,12 @@ __device__ __forceinline__ float fmaR(float a, float b, float c) {
 //               closed form, perfect crystal, or a grid that cannot be
 //               staged asynchronously);
 //   ST_DIRECT   staged e^{iH} rows of the march's own precision are copied
-//               with cp.async two steps ahead into three stages and read in
-//               place by the update;
+//               two steps ahead into three stages and read in place by the
+//               update (the staged march: one thread's bulk copy a row;
+//               the generic march: every thread's cp.async);
 //   ST_CONVERT  raw rows (H grids, or e^{iH} of the other precision) are
-//               copied the same way and turned into e^{iH} by the producer.
+//               copied with cp.async and turned into e^{iH} by the
+//               producer.
 enum StageMode { ST_COMPUTE = 0, ST_DIRECT = 1, ST_CONVERT = 2 };
 
 // Shared-memory plan of the march kernel (bytes), shared with the host.
@@ -440,8 +442,10 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         hcr = reduce_2pi(hconst);
     }
 
-    // Asynchronous copy of the raw row of step kk into stage kk % 3; every
-    // thread commits one group per call, copy or not.
+    // Asynchronous copy of the raw row of step kk into stage kk % 3: the
+    // staged march's thread 0 issues one bulk copy; otherwise every thread
+    // copies its 16-byte chunks and commits one group per call, copy or
+    // not.
     const unsigned char *raw_src = nullptr;
     size_t raw_row = 0;
     if (stage != ST_COMPUTE) {
