@@ -216,7 +216,9 @@ __host__ __device__ inline MarchSmem march_smem(int CPL, int WA, int A,
         ? ((ncols * raw_elem + 15) & ~(size_t)15) : 0;
     off += 3 * m.raw_stage;
     m.bnd = off;
-    off += (size_t)3 * nwarps * (comp ? 4 : 2) * sizeof(R2);
+    // three ring stages of slots a warp, and one slot of zeros (the
+    // missing neighbour of a row's first and last warp)
+    off += (size_t)(3 * nwarps + 1) * (comp ? 4 : 2) * sizeof(R2);
     off = (off + 15) & ~(size_t)15;
     m.an = off;
     if (hsrc == HS_ANALYTIC) off += (size_t)Nz * sizeof(R2);
@@ -293,6 +295,43 @@ static __device__ __noinline__ bool row_bar_wait_slow(unsigned long long *bar,
 __device__ __forceinline__ bool row_bar_wait(unsigned long long *bar,
                                              unsigned parity) {
     return row_bar_try(bar, parity) || row_bar_wait_slow(bar, parity);
+}
+
+// Predicated shared-memory accesses of a boundary slot: only the lanes with
+// p load (keeping their registers otherwise) or store, with no branch.
+__device__ __forceinline__ void ld_shared_if(bool p, const float2 *a,
+                                             float &x, float &y) {
+    asm volatile(
+        "{\n .reg .pred q;\n setp.ne.u32 q, %2, 0;\n"
+        " @q ld.shared.v2.f32 {%0, %1}, [%3];\n}\n"
+        : "+f"(x), "+f"(y)
+        : "r"((unsigned)p), "r"(smem_addr(a))
+        : "memory");
+}
+__device__ __forceinline__ void ld_shared_if(bool p, const double2 *a,
+                                             double &x, double &y) {
+    asm volatile(
+        "{\n .reg .pred q;\n setp.ne.u32 q, %2, 0;\n"
+        " @q ld.shared.v2.f64 {%0, %1}, [%3];\n}\n"
+        : "+d"(x), "+d"(y)
+        : "r"((unsigned)p), "r"(smem_addr(a))
+        : "memory");
+}
+__device__ __forceinline__ void st_shared_if(bool p, float2 *a, float x,
+                                             float y) {
+    asm volatile(
+        "{\n .reg .pred q;\n setp.ne.u32 q, %0, 0;\n"
+        " @q st.shared.v2.f32 [%1], {%2, %3};\n}\n" ::"r"((unsigned)p),
+        "r"(smem_addr(a)), "f"(x), "f"(y)
+        : "memory");
+}
+__device__ __forceinline__ void st_shared_if(bool p, double2 *a, double x,
+                                             double y) {
+    asm volatile(
+        "{\n .reg .pred q;\n setp.ne.u32 q, %0, 0;\n"
+        " @q st.shared.v2.f64 [%1], {%2, %3};\n}\n" ::"r"((unsigned)p),
+        "r"(smem_addr(a)), "d"(x), "d"(y)
+        : "memory");
 }
 
 __device__ __forceinline__ void cp_async16(void *dst_smem, const void *src) {
@@ -410,6 +449,8 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         for (int st = 0; st < 3; ++st) row_bar_init(&bars[st]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    if (kStaged && tid < NB)     // the zero slot of the missing neighbours
+        bnd[3 * nwarps * NB + tid] = R2{R(0), R(0)};
     if (stage == ST_DIRECT) {
         // Columns beyond Nx of every stage read as zero coupling.
         for (int st = 0; st < 3; ++st) {
@@ -641,8 +682,10 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         for (int r = 0; r < 3; ++r) {
             st_src[r] = reinterpret_cast<const R2 *>(
                             raw + (size_t)r * plan.raw_stage) + L * CPL;
-            st_next[r] = bnd + (r * nwarps + nb_next) * NB;
-            st_prev[r] = bnd + (r * nwarps + nb_prev) * NB;
+            st_next[r] = has_next ? bnd + (r * nwarps + nb_next) * NB
+                                  : bnd + 3 * nwarps * NB;   // zeros
+            st_prev[r] = has_prev ? bnd + (r * nwarps + nb_prev) * NB
+                                  : bnd + 3 * nwarps * NB;
             st_own[r] = bnd + (r * nwarps + warp) * NB + (is_first ? 0 : 1);
         }
     }
@@ -679,17 +722,20 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
             binlr = __shfl_up_sync(0xffffffffu, Blr[CPL - 1], 1);
             binli = __shfl_up_sync(0xffffffffu, Bli[CPL - 1], 1);
         }
-        // Every lane reads the same boundary slots (a broadcast) and lanes
-        // 31 and 0 keep them by selection, with no branch.
-        {
-            const R2 *nxt, *prv;
-            if constexpr (kStaged) {
-                nxt = st_next[ring];
-                prv = st_prev[ring];
-            } else {
-                nxt = bnd + (ring * nwarps + nb_next) * NB;
-                prv = bnd + (ring * nwarps + nb_prev) * NB;
+        if constexpr (kStaged) {
+            // lane 31 loads the next warp's A(0), lane 0 the previous
+            // warp's B(CPL - 1) (zeros at the row's ends)
+            ld_shared_if(is_last, st_next[ring] + 0, ainr, aini);
+            ld_shared_if(is_first, st_prev[ring] + 1, binr, bini);
+            if constexpr (COMP) {
+                ld_shared_if(is_last, st_next[ring] + 2, ainlr, ainli);
+                ld_shared_if(is_first, st_prev[ring] + 3, binlr, binli);
             }
+        } else {
+            // every lane reads the same slots (a broadcast) and lanes 31
+            // and 0 keep them by selection, with no branch
+            const R2 *nxt = bnd + (ring * nwarps + nb_next) * NB;
+            const R2 *prv = bnd + (ring * nwarps + nb_prev) * NB;
             const R2 t = nxt[0];
             const R2 v = prv[1];
             ainr = is_last ? (has_next ? t.x : R(0)) : ainr;
@@ -758,13 +804,18 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                 Alr[j] = e0; Ali[j] = e1; Blr[j] = e2; Bli[j] = e3;
             }
         }
-        // lane 0 publishes its A(0), lane 31 its B(CPL - 1) (one branch)
-        if (is_first || is_last) {
-            R2 *slot;
-            if constexpr (kStaged)
-                slot = st_own[nslot];
-            else
-                slot = bnd + (nslot * nwarps + warp) * NB + (is_first ? 0 : 1);
+        // lane 0 publishes its A(0), lane 31 its B(CPL - 1)
+        if constexpr (kStaged) {
+            const bool pub = is_first || is_last;
+            st_shared_if(pub, st_own[nslot], is_first ? Ar[0] : Br[CPL - 1],
+                         is_first ? Ai[0] : Bi[CPL - 1]);
+            if constexpr (COMP)
+                st_shared_if(pub, st_own[nslot] + 2,
+                             is_first ? Alr[0] : Blr[CPL - 1],
+                             is_first ? Ali[0] : Bli[CPL - 1]);
+        } else if (is_first || is_last) {
+            R2 *slot =
+                bnd + (nslot * nwarps + warp) * NB + (is_first ? 0 : 1);
             slot[0] = is_first ? R2{Ar[0], Ai[0]} : R2{Br[CPL - 1], Bi[CPL - 1]};
             if constexpr (COMP)
                 slot[2] = is_first ? R2{Alr[0], Ali[0]}
