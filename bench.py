@@ -60,7 +60,7 @@ README_WORKLOAD = ("laue-readme: diamond(400) 17 keV, t=200um dx=0.25um "
 # laue_march_kernel<float, 11, staged e^{iH}, compensated>: an ncu capture
 # of the full 256-angle launch (`python bench.py --once scan256`: the staged
 # e^{iH} table, 2.0 GB, read once, and the 1.0 GB of exit waves written).
-MARCH_SCAN_DRAM_BYTES = 2011973120 + 1025791488
+MARCH_SCAN_DRAM_BYTES = 2007279872 + 1023596544
 MARCH_SCAN_DRAM_SHAPE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum "
                          "of the 256-angle march launch (11 columns per "
                          "lane, 4 angles per CTA: the block's register "
