@@ -449,7 +449,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         for (int st = 0; st < 3; ++st) row_bar_init(&bars[st]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (kStaged && tid < NB)     // the zero slot of the missing neighbours
+    if (tid < NB)                // the zero slot of the missing neighbours
         bnd[3 * nwarps * NB + tid] = R2{R(0), R(0)};
     if (stage == ST_DIRECT) {
         // Columns beyond Nx of every stage read as zero coupling.
@@ -722,33 +722,41 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
             binlr = __shfl_up_sync(0xffffffffu, Blr[CPL - 1], 1);
             binli = __shfl_up_sync(0xffffffffu, Bli[CPL - 1], 1);
         }
-        if constexpr (kStaged) {
-            // lane 31 loads the next warp's A(0), lane 0 the previous
-            // warp's B(CPL - 1) (zeros at the row's ends)
-            ld_shared_if(is_last, st_next[ring] + 0, ainr, aini);
-            ld_shared_if(is_first, st_prev[ring] + 1, binr, bini);
-            if constexpr (COMP) {
-                ld_shared_if(is_last, st_next[ring] + 2, ainlr, ainli);
-                ld_shared_if(is_first, st_prev[ring] + 3, binlr, binli);
+        // lane 31 loads the next warp's A(0), lane 0 the previous warp's
+        // B(CPL - 1) (zeros at the row's ends): predicated loads, or (the
+        // fused FP64-sum march, where they cost registers) broadcast loads
+        // that those two lanes keep by selection
+        {
+            const R2 *nxt, *prv;
+            if constexpr (kStaged) {
+                nxt = st_next[ring];
+                prv = st_prev[ring];
+            } else {
+                nxt = has_next ? bnd + (ring * nwarps + nb_next) * NB
+                               : bnd + 3 * nwarps * NB;
+                prv = has_prev ? bnd + (ring * nwarps + nb_prev) * NB
+                               : bnd + 3 * nwarps * NB;
             }
-        } else {
-            // every lane reads the same slots (a broadcast) and lanes 31
-            // and 0 keep them by selection, with no branch
-            const R2 *nxt = bnd + (ring * nwarps + nb_next) * NB;
-            const R2 *prv = bnd + (ring * nwarps + nb_prev) * NB;
-            const R2 t = nxt[0];
-            const R2 v = prv[1];
-            ainr = is_last ? (has_next ? t.x : R(0)) : ainr;
-            aini = is_last ? (has_next ? t.y : R(0)) : aini;
-            binr = is_first ? (has_prev ? v.x : R(0)) : binr;
-            bini = is_first ? (has_prev ? v.y : R(0)) : bini;
-            if constexpr (COMP) {
-                const R2 u = nxt[2];
-                const R2 w = prv[3];
-                ainlr = is_last ? (has_next ? u.x : R(0)) : ainlr;
-                ainli = is_last ? (has_next ? u.y : R(0)) : ainli;
-                binlr = is_first ? (has_prev ? w.x : R(0)) : binlr;
-                binli = is_first ? (has_prev ? w.y : R(0)) : binli;
+            if constexpr (HT != HT_SEG64) {
+                ld_shared_if(is_last, nxt + 0, ainr, aini);
+                ld_shared_if(is_first, prv + 1, binr, bini);
+                if constexpr (COMP) {
+                    ld_shared_if(is_last, nxt + 2, ainlr, ainli);
+                    ld_shared_if(is_first, prv + 3, binlr, binli);
+                }
+            } else {
+                const R2 t = nxt[0], v = prv[1];
+                ainr = is_last ? t.x : ainr;
+                aini = is_last ? t.y : aini;
+                binr = is_first ? v.x : binr;
+                bini = is_first ? v.y : bini;
+                if constexpr (COMP) {
+                    const R2 u = nxt[2], w = prv[3];
+                    ainlr = is_last ? u.x : ainlr;
+                    ainli = is_last ? u.y : ainli;
+                    binlr = is_first ? w.x : binlr;
+                    binli = is_first ? w.y : binli;
+                }
             }
         }
         const R2 *src;
@@ -805,21 +813,27 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
             }
         }
         // lane 0 publishes its A(0), lane 31 its B(CPL - 1)
-        if constexpr (kStaged) {
+        {
+            R2 *slot;
+            if constexpr (kStaged)
+                slot = st_own[nslot];
+            else
+                slot = bnd + (nslot * nwarps + warp) * NB + (is_first ? 0 : 1);
             const bool pub = is_first || is_last;
-            st_shared_if(pub, st_own[nslot], is_first ? Ar[0] : Br[CPL - 1],
-                         is_first ? Ai[0] : Bi[CPL - 1]);
-            if constexpr (COMP)
-                st_shared_if(pub, st_own[nslot] + 2,
-                             is_first ? Alr[0] : Blr[CPL - 1],
-                             is_first ? Ali[0] : Bli[CPL - 1]);
-        } else if (is_first || is_last) {
-            R2 *slot =
-                bnd + (nslot * nwarps + warp) * NB + (is_first ? 0 : 1);
-            slot[0] = is_first ? R2{Ar[0], Ai[0]} : R2{Br[CPL - 1], Bi[CPL - 1]};
-            if constexpr (COMP)
-                slot[2] = is_first ? R2{Alr[0], Ali[0]}
-                                   : R2{Blr[CPL - 1], Bli[CPL - 1]};
+            if constexpr (HT != HT_SEG64) {
+                st_shared_if(pub, slot, is_first ? Ar[0] : Br[CPL - 1],
+                             is_first ? Ai[0] : Bi[CPL - 1]);
+                if constexpr (COMP)
+                    st_shared_if(pub, slot + 2,
+                                 is_first ? Alr[0] : Blr[CPL - 1],
+                                 is_first ? Ali[0] : Bli[CPL - 1]);
+            } else if (pub) {
+                slot[0] = is_first ? R2{Ar[0], Ai[0]}
+                                   : R2{Br[CPL - 1], Bi[CPL - 1]};
+                if constexpr (COMP)
+                    slot[2] = is_first ? R2{Alr[0], Ali[0]}
+                                       : R2{Blr[CPL - 1], Bli[CPL - 1]};
+            }
         }
         // The stage of step k + 1 (DIRECT) or k + 2 (CONVERT) is complete
         // and, after the barrier, visible to every thread.
