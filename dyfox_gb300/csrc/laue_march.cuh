@@ -724,8 +724,11 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
         }
         // lane 31 loads the next warp's A(0), lane 0 the previous warp's
         // B(CPL - 1) (zeros at the row's ends): predicated loads, or (the
-        // fused FP64-sum march, where they cost registers) broadcast loads
-        // that those two lanes keep by selection
+        // fused marches with FP64 sum or few columns per lane, where those
+        // cost registers and occupancy) broadcast loads that the two lanes
+        // keep by selection
+        constexpr bool kPredBnd =
+            HT != HT_SEG64 && !(HT == HT_SEG && CPL < 7);
         {
             const R2 *nxt, *prv;
             if constexpr (kStaged) {
@@ -737,7 +740,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
                 prv = has_prev ? bnd + (ring * nwarps + nb_prev) * NB
                                : bnd + 3 * nwarps * NB;
             }
-            if constexpr (HT != HT_SEG64) {
+            if constexpr (kPredBnd) {
                 ld_shared_if(is_last, nxt + 0, ainr, aini);
                 ld_shared_if(is_first, prv + 1, binr, bini);
                 if constexpr (COMP) {
@@ -820,7 +823,7 @@ __device__ __forceinline__ void march_block(const MarchArgs &a, int row_blk,
             else
                 slot = bnd + (nslot * nwarps + warp) * NB + (is_first ? 0 : 1);
             const bool pub = is_first || is_last;
-            if constexpr (HT != HT_SEG64) {
+            if constexpr (kPredBnd) {
                 st_shared_if(pub, slot, is_first ? Ar[0] : Br[CPL - 1],
                              is_first ? Ai[0] : Bi[CPL - 1]);
                 if constexpr (COMP)
