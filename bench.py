@@ -706,7 +706,7 @@ def run_once(args):
         return
     if args.once in ("bragg", "bragg32", "bragg32-scan"):
         # 4 deviation parameters x 8 planes, or (bragg32-scan) the whole
-        # config-1 scan, 21 x 64, in mixed precision
+        # 20 um scan, 21 x 64, in mixed precision
         from dyfox_gb300.bragg import solve_scan
         bx, bcfg, bseg, bs, bys, bg = bragg_workload()
         prec = "fp64" if args.once == "bragg" else "fp32"
@@ -1358,9 +1358,10 @@ def bragg_flops(inf, Nx, Nz, restart):
 
 
 def bragg_leg(args, rank, world, peaks=None):
-    """Bragg solves/s of config 1: all 21 deviation parameters x 64 planes
-    in one batched launch (one solve = one deviation parameter over all
-    planes, to true relative residual <= 1e-10).  The chosen form is the
+    """Bragg solves/s of the 20 um scan (diamond (400), Nx 456, Nz 90): all
+    21 deviation parameters x 64 planes in one batched launch (one solve =
+    one deviation parameter over all planes, to true relative residual
+    <= 1e-10).  The chosen form is the
     mixed-precision solve (single-precision Krylov products, float-float
     right-hand side and true residuals, double Gram-Schmidt and solution);
     plain FP64 is timed beside it, and the two answers are compared."""

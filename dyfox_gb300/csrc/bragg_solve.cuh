@@ -347,7 +347,8 @@ __device__ __forceinline__ void resume_system(const BraggArgs &a, int sys,
 
 // The GMRES kernels carry no launch bounds: the compiler's own choice
 // (about 100 registers for the 4-column mixed kernel) measured fastest on
-// config 1.  Bounds of (128, 5) forced 96 registers and lost 18%; bounds of
+// the 20 um Bragg scan (Nx 456, Nz 90, 21 x 64 systems).  Bounds of
+// (128, 5) forced 96 registers and lost 18%; bounds of
 // (NT, 1) let it take 212 registers and lost 40% to occupancy.
 
 // One CTA of NT threads per system of one solve call.
@@ -358,8 +359,9 @@ bragg_gmres_kernel(const BraggArgs a) {
     solve_system<CPL, MIXED>(a, blockIdx.x, smem);
 }
 
-// The mixed 4-column, 128-thread kernel (config 1's shape) with bounds that
-// keep 5 CTAs per SM (96 registers instead of 122: 4% on config 1).  Bounds
+// The mixed 4-column, 128-thread kernel (the shape of the 20 um scan's
+// 456-column planes) with bounds that keep 5 CTAs per SM (96 registers
+// instead of 122: 4% on that scan).  Bounds
 // on every instantiation would let the others take 186-234 registers.
 // (a template so that only the unit that launches it compiles it)
 template <int NT>
