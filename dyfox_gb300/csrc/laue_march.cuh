@@ -895,12 +895,37 @@ __global__ void laue_march_kernel(const MarchArgs a) {
                                   blockIdx.x - row_blk * a.n_groups, smem);
 }
 
+// The same with at most 80 registers a thread: the fused single-precision
+// marches at 5 columns per lane run two 320-thread CTAs per multiprocessor
+// at 80 registers, and the compiler's own allocation for them moves with
+// small changes to the phase code and can cost that second CTA.
+template <typename R, int CPL, int HT, bool COMP>
+__global__ void __maxnreg__(80) laue_march_kernel_r80(const MarchArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int row_blk = blockIdx.x / a.n_groups;
+    march_block<R, CPL, HT, COMP>(a, row_blk,
+                                  blockIdx.x - row_blk * a.n_groups, smem);
+}
+
+template <typename R, int CPL, int HT, bool COMP>
+constexpr bool march_capped() {
+    return sizeof(R) == 4 && CPL == 5 && (HT == HT_SEG || HT == HT_SEG64);
+}
+
+template <typename R, int CPL, int HT, bool COMP>
+constexpr auto march_kernel() {
+    if constexpr (march_capped<R, CPL, HT, COMP>())
+        return laue_march_kernel_r80<R, CPL, HT, COMP>;
+    else
+        return laue_march_kernel<R, CPL, HT, COMP>;
+}
+
 // Host launch of one instantiation; returns cudaError_t.  Also reports the
 // instantiation's maximum block size and register count.
 template <typename R, int CPL, int HT, bool COMP>
 cudaError_t launch_march(const MarchArgs &a, int grid, int block, size_t smem,
                          cudaStream_t stream) {
-    auto *k = laue_march_kernel<R, CPL, HT, COMP>;
+    auto *k = march_kernel<R, CPL, HT, COMP>();
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -913,7 +938,7 @@ cudaError_t launch_march(const MarchArgs &a, int grid, int block, size_t smem,
 
 template <typename R, int CPL, int HT, bool COMP>
 cudaError_t attr_march(cudaFuncAttributes *attr) {
-    return cudaFuncGetAttributes(attr, laue_march_kernel<R, CPL, HT, COMP>);
+    return cudaFuncGetAttributes(attr, march_kernel<R, CPL, HT, COMP>());
 }
 
 using MarchLaunch = cudaError_t (*)(const MarchArgs &, int, int, size_t,
